@@ -1,0 +1,28 @@
+// aph_capi_internal.h -- helpers shared by the C-ABI translation units.
+#pragma once
+#include <cstdarg>
+#include <vector>
+
+#include "../../include/aph_hydro.h"
+#include "aph_internal.h"
+
+namespace aph {
+aph_status fail(aph_status code, const char *fmt, ...);
+aph_status cuda_fail(cudaError_t e, const char *where);
+void clear_error();
+const char *last_error();
+void fill_gas_consts(PackDev &p);
+aph_status validate_params(const aph_hydro_params *params);
+
+const BlockDev *pack_blocks(aph_pack p);
+const PackDev &pack_dev(aph_pack p);
+int pack_max_interior(aph_pack p);
+int pack_max_ncell(aph_pack p);
+const aph_hydro_params &pack_params(aph_pack p);
+const std::vector<BlockDev> &pack_host_blocks(aph_pack p);
+bool pack_has_topology(aph_pack p);
+
+// field: 0 cons, 1 u1
+cudaError_t launch_fill_ghosts(const PackDev &p, const BlockDev *blocks, int max_ncell, int field,
+                               cudaStream_t s);
+}  // namespace aph

@@ -1,0 +1,463 @@
+// aph_math.cuh -- device arithmetic of the hydro flux path (sm_103a).
+//
+// On GB300 every FP64 instruction -- add, mul, fma, but also compare (DSETP) and
+// min/max -- goes through a pipe that retires about two warp-lanes per clock per SM,
+// while the integer and FP32 pipes run about sixty times faster.  The predicates and
+// min/max below therefore work on the IEEE bit patterns with integer instructions.
+// They give the same answer as the IEEE comparison for every non-NaN input, -0.0 and
+// +0.0 included, so using them changes no result bit.
+//
+// APH_EXACT selects the arithmetic:
+//   1  the reference's operation order, one rounding per operation (the translation
+//      unit is built with --fmad=false); bit-identical to the reference's FP64 CPU path.
+//   0  the same algorithm with fused multiply-adds, shared reciprocals and
+//      precomputed gamma-dependent constants; agrees to ~1e-15 relative per operation.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#ifndef APH_EXACT
+#define APH_EXACT 0
+#endif
+
+namespace aph {
+
+constexpr int IDN = 0, IM1 = 1, IM2 = 2, IM3 = 3, IEN = 4, NHYDRO = 5;
+constexpr int IV1 = 1, IV2 = 2, IV3 = 3, IPR = 4;
+constexpr int RECON_DC = 1, RECON_PLM = 2, RECON_PPM = 3;
+constexpr int RS_NONE = 1, RS_HLLE = 2, RS_HLLC = 3, RS_LHLLC = 4;
+
+constexpr double C_LIGHT = 2.99792458e10;        // hydro_hlle.hpp:26
+constexpr double C_LIGHT2 = C_LIGHT * C_LIGHT;   // SQR(C_LIGHT)
+constexpr double TINY_NUMBER = 1.0e-20;
+constexpr double PPM_C2 = 1.25;                  // ppm_simple.hpp:36
+
+// ---- integer-pipe predicates ------------------------------------------------
+__device__ __forceinline__ bool is_neg(double x) {  // x < 0.0
+  const int hi = __double2hiint(x), lo = __double2loint(x);
+  return hi < 0 && ((((unsigned)hi) << 1) | (unsigned)lo) != 0u;
+}
+__device__ __forceinline__ bool is_pos(double x) {  // x > 0.0
+  const int hi = __double2hiint(x), lo = __double2loint(x);
+  return hi >= 0 && (hi | lo) != 0;
+}
+// monotone integer key: a < b  <=>  okey(a) < okey(b)  (-0.0 and +0.0 share key 0)
+__device__ __forceinline__ long long okey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b >= 0 ? b : (long long)(0x8000000000000000ULL - (unsigned long long)b);
+}
+__device__ __forceinline__ bool lt(double a, double b) { return okey(a) < okey(b); }
+__device__ __forceinline__ bool le(double a, double b) { return okey(a) <= okey(b); }
+__device__ __forceinline__ bool gt(double a, double b) { return okey(a) > okey(b); }
+// std::min / std::max tie rules (the first argument wins when neither is smaller)
+__device__ __forceinline__ double smin(double a, double b) { return lt(b, a) ? b : a; }
+__device__ __forceinline__ double smax(double a, double b) { return lt(a, b) ? b : a; }
+__device__ __forceinline__ unsigned long long mag(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ double dabs(double x) { return __longlong_as_double((long long)mag(x)); }
+// bits of 2*|x| (exact doubling: exponent +1, or a shift for subnormals; overflow -> inf)
+__device__ __forceinline__ unsigned long long twice_mag(double x) {
+  const unsigned long long m = mag(x);
+  const unsigned long long e = m >> 52;
+  if (e == 0) return m << 1;
+  if (e >= 0x7feULL) return 0x7ff0000000000000ULL;
+  return m + (1ULL << 52);
+}
+// v with its sign flipped when neg (SIGN(s) * v for SIGN in {-1, +1})
+__device__ __forceinline__ double flip_if(double v, bool neg) {
+  return neg ? __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ULL) : v;
+}
+__device__ __forceinline__ double from_bits(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// ---- gamma-dependent constants of a pack (fast mode) ---------------------------
+struct GasConsts {
+  double gm1, igm1, gamma;      // eos/gm1, 1/gm1, gm1+1
+  double c2g;                   // C^2 * gamma
+  double one_igm1;              // 1 + 1/gm1
+  double hlle_k;                // (gamma+1)/sqrt(2 gamma)
+  double hllc_k;                // (gamma+1)/(2 gamma)
+};
+
+// ---- ideal gas (singularity-eos IdealGas) ------------------------------------
+__device__ __forceinline__ double eos_pressure(double gm1, double rho, double sie) {
+  const double p = gm1 * rho * sie;
+  return is_neg(p) ? 0.0 : p;
+}
+__device__ __forceinline__ double eos_bulk_modulus(double gm1, double rho, double sie) {
+  const double small = 10.0 * 2.2250738585072014e-308;
+  const double b = gm1 * (gm1 + 1.0) * rho * sie;
+  return lt(small, b) ? b : small;
+}
+
+// ConsToPrim for one cell (hydro.cpp:459-531, ideal gas).  u[] is updated in place
+// by the floors (density, energy); w[] gets rho, v1, v2, v3, p; g_c, g_e the two
+// adiabatic indices.  Returns true when the pressure floor was applied.
+__device__ __forceinline__ bool cons_to_prim_cell(double *u, double *w, double &g_c, double &g_e,
+                                                  double gm1, double dfloor, double pfloor) {
+  double u_d = u[IDN];
+  u_d = gt(u_d, dfloor) ? u_d : dfloor;
+  u[IDN] = u_d;
+  const double di = 1.0 / u_d;
+  w[IDN] = u_d;
+  w[IV1] = u[IM1] * di;
+  w[IV2] = u[IM2] * di;
+  w[IV3] = u[IM3] * di;
+  const double e_k = 0.5 * di * (u[IM1] * u[IM1] + u[IM2] * u[IM2] + u[IM3] * u[IM3]);
+  double u_e = u[IEN];
+  double w_p = eos_pressure(gm1, u_d, (u_e - e_k) / u_d);
+  const bool floored = !gt(w_p, pfloor);
+  if (floored) {
+    const double gm1q = w_p / (u_d * e_k);  // hydro.cpp:517
+    u_e = (pfloor / gm1q) + e_k;
+    w_p = pfloor;
+  }
+  u[IEN] = u_e;
+  w[IPR] = w_p;
+  g_c = eos_bulk_modulus(gm1, u_d, (u_e - e_k) / u_d) / w_p;
+  g_e = w_p / (u_e - e_k) + 1;
+  return floored;
+}
+
+// ---- reconstruction (src/recon) --------------------------------------------------
+__device__ __forceinline__ void plm(double q_im1, double q_i, double q_ip1, double &ql_ip1,
+                                    double &qr_i) {
+  const double dql = q_i - q_im1;
+  const double dqr = q_ip1 - q_i;
+  const double dq2 = dql * dqr;
+  double dqm = 0.0;
+  if (is_pos(dq2)) dqm = dq2 / (dql + dqr);
+  ql_ip1 = q_i + dqm;
+  qr_i = q_i - dqm;
+}
+
+// PPM split in two.  The limited interface value at a face is a function of the four
+// cells around it only, and the reference computes it identically from both adjacent
+// cells (its symmetric grouping of the stencil sums makes the two evaluations the same
+// operations on the same operands).  ppm_face() evaluates it once per face;
+// ppm_cell() then applies the cell's parabola limiter.  Together they give exactly
+// PPM(q_im2..q_ip2) of ppm_simple.hpp:32-161.
+//
+// dd(c) = 0.5*(q[c+1]-q[c]) + 0.5*(q[c]-q[c-1]);  d2(c) = (q[c-1]+q[c+1]) - 2*q[c]
+__device__ __forceinline__ double ppm_dd(double qm1, double q0, double qp1) {
+  return 0.5 * (qp1 - q0) + 0.5 * (q0 - qm1);
+}
+__device__ __forceinline__ double ppm_d2(double qm1, double q0, double qp1) {
+  return (qm1 + qp1) - 2.0 * q0;
+}
+// Face between cells c-1 (value qm1) and c (value q0): ddm1 = dd(c-1), dd0 = dd(c),
+// d2m1 = d2(c-1), d20 = d2(c).
+__device__ __forceinline__ double ppm_face(double qm1, double q0, double ddm1, double dd0,
+                                           double d2m1, double d20) {
+  const double avg = 0.5 * (qm1 + q0);
+#if APH_EXACT
+  double dph = avg + (ddm1 - dd0) / 6.0;
+#else
+  double dph = fma(ddm1 - dd0, 1.0 / 6.0, avg);
+#endif
+  const double qa_tmp = dph - qm1;
+  const double qb_tmp = q0 - dph;
+  const double qa = 3.0 * (qm1 + q0 - 2.0 * dph);
+  double qd = 0.0;
+  const bool sa = is_neg(qa);
+  if (sa == is_neg(d2m1) && sa == is_neg(d20)) {
+    // min(C2|qb|, min(C2|qc|, |qa|)) with the two scalings merged (scaling by a positive
+    // constant is monotone, so min(C2 x, C2 y) == C2 min(x, y) bit for bit)
+    const unsigned long long mb = mag(d2m1), mc = mag(d20);
+    const double m = PPM_C2 * from_bits(mc < mb ? mc : mb);
+    const unsigned long long mm = mag(m), ma = mag(qa);
+    qd = flip_if(from_bits(ma < mm ? ma : mm), sa);
+  }
+  if (is_neg(qa_tmp * qb_tmp)) {
+#if APH_EXACT
+    dph = avg - qd / 6.0;
+#else
+    dph = fma(qd, -1.0 / 6.0, avg);
+#endif
+  }
+  return dph;
+}
+
+// Cell limiter: dph_lo, dph_hi are the limited values at faces i-1/2, i+1/2.
+// Outputs ql_ip1 (left state of face i+1/2) and qr_i (right state of face i-1/2).
+__device__ __forceinline__ void ppm_cell(double q_im2, double q_im1, double q_i, double q_ip1,
+                                         double q_ip2, double d2m1, double d20, double d2p1,
+                                         double dph_lo, double dph_hi, double &ql_ip1,
+                                         double &qr_i) {
+  const double d2qf = 6.0 * (dph_lo + dph_hi - 2.0 * q_i);
+  double qr = dph_lo, ql = dph_hi;
+  const double dqf_minus = q_i - qr;
+  const double dqf_plus = ql - q_i;
+  const double qa_tmp = dqf_minus * dqf_plus;
+  const double qb_tmp = (q_ip1 - q_i) * (q_i - q_im1);
+  if (!is_pos(qa_tmp) || !is_pos(qb_tmp)) {
+    // local extremum: limit with rho = qe/qd (CS eq 22-23, MC eq 27)
+    double qe = 0.0;
+    const bool sd = is_neg(d2qf);
+    if (sd == is_neg(d2m1) && sd == is_neg(d20) && sd == is_neg(d2p1)) {
+      unsigned long long m = mag(d2m1);
+      const unsigned long long m0 = mag(d20), m1 = mag(d2p1);
+      m = m0 < m ? m0 : m;
+      m = m1 < m ? m1 : m;
+      const unsigned long long ms = mag(PPM_C2 * from_bits(m)), md = mag(d2qf);
+      qe = flip_if(from_bits(md < ms ? md : ms), sd);
+    }
+    unsigned long long mx = mag(q_im2);
+    const unsigned long long a1 = mag(q_im1), a2 = mag(q_i), a3 = mag(q_ip1), a4 = mag(q_ip2);
+    mx = a1 > mx ? a1 : mx;
+    mx = a2 > mx ? a2 : mx;
+    mx = a3 > mx ? a3 : mx;
+    mx = a4 > mx ? a4 : mx;
+    double rho = 0.0;
+    if (mag(d2qf) > mag(1.0e-12 * from_bits(mx))) rho = qe / d2qf;
+    if (le(rho, 1.0 - 1.0e-12)) {
+#if APH_EXACT
+      qr = q_i - rho * dqf_minus;
+      ql = q_i + rho * dqf_plus;
+#else
+      qr = fma(-rho, dqf_minus, q_i);
+      ql = fma(rho, dqf_plus, q_i);
+#endif
+    }
+  } else {
+    if (mag(dqf_minus) >= twice_mag(dqf_plus)) qr = q_i - 2.0 * dqf_plus;
+    if (mag(dqf_plus) >= twice_mag(dqf_minus)) ql = q_i + 2.0 * dqf_minus;
+  }
+  ql_ip1 = ql;
+  qr_i = qr;
+}
+
+// Whole-cell PPM from the five-point stencil (used where the face values are not shared).
+__device__ __forceinline__ void ppm(double q_im2, double q_im1, double q_i, double q_ip1,
+                                    double q_ip2, double &ql_ip1, double &qr_i) {
+  const double dd_m1 = ppm_dd(q_im2, q_im1, q_i);
+  const double dd_0 = ppm_dd(q_im1, q_i, q_ip1);
+  const double dd_p1 = ppm_dd(q_i, q_ip1, q_ip2);
+  const double d2_m1 = ppm_d2(q_im2, q_im1, q_i);
+  const double d2_0 = ppm_d2(q_im1, q_i, q_ip1);
+  const double d2_p1 = ppm_d2(q_i, q_ip1, q_ip2);
+  const double lo = ppm_face(q_im1, q_i, dd_m1, dd_0, d2_m1, d2_0);
+  const double hi = ppm_face(q_i, q_ip1, dd_0, dd_p1, d2_0, d2_p1);
+  ppm_cell(q_im2, q_im1, q_i, q_ip1, q_ip2, d2_m1, d2_0, d2_p1, lo, hi, ql_ip1, qr_i);
+}
+
+template <int RECON>
+__device__ __forceinline__ void reconstruct(const double *q, double &ql_ip1, double &qr_i) {
+  // q[-2..2] addressable around q[0]
+  if (RECON == RECON_DC) {
+    ql_ip1 = qr_i = q[0];
+  } else if (RECON == RECON_PLM) {
+    plm(q[-1], q[0], q[1], ql_ip1, qr_i);
+  } else {
+    ppm(q[-2], q[-1], q[0], q[1], q[2], ql_ip1, qr_i);
+  }
+}
+
+// ---- Riemann solvers (src/hydro/rsolvers) -------------------------------------------
+// wl, wr: (rho, v_normal, v_t1, v_t2, p).  gl*, gr*: reconstructed (gamma_c, gamma_e).
+// With CONSTG the adiabatic indices are the pack's constants (gc) instead.
+// flx: (mass, normal momentum, t1 momentum, t2 momentum, energy).
+
+// c-limited sound speed C*sqrt(gamma / (1 + (1/gm1 + rho C^2 / p))) (hydro_hlle.hpp:63-66)
+template <bool CONSTG>
+__device__ __forceinline__ double sound_speed(double rho, double p, double gamma, double igm1,
+                                              const GasConsts &gc) {
+#if APH_EXACT
+  return C_LIGHT * sqrt(gamma / (1 + (igm1 + rho * C_LIGHT2 / p)));
+#else
+  // same quantity as sqrt(C^2 gamma p / (p (1 + 1/gm1) + rho C^2))
+  const double num = (CONSTG ? gc.c2g : C_LIGHT2 * gamma) * p;
+  const double den = fma(p, CONSTG ? gc.one_igm1 : 1.0 + igm1, rho * C_LIGHT2);
+  return num * rsqrt(num * den);
+#endif
+}
+
+template <bool CONSTG>
+__device__ __forceinline__ void solve_hlle(const double *wli, const double *wri, double glc,
+                                           double gle, double grc, double gre,
+                                           const GasConsts &gc, double *flxi) {
+  const double gammal = CONSTG ? gc.gamma : glc;
+  const double gammar = CONSTG ? gc.gamma : grc;
+  double igm1l, igm1r;
+  if (CONSTG) {
+    igm1l = igm1r = gc.igm1;
+  } else {
+    igm1l = 1.0 / (gle - 1);
+    igm1r = 1.0 / (gre - 1);
+  }
+  const double cl = sound_speed<CONSTG>(wli[IDN], wli[IPR], gammal, igm1l, gc);
+  const double cr = sound_speed<CONSTG>(wri[IDN], wri[IPR], gammar, igm1r, gc);
+  const double el = wli[IPR] * igm1l +
+                    0.5 * wli[IDN] * (wli[IV1] * wli[IV1] + wli[IV2] * wli[IV2] + wli[IV3] * wli[IV3]);
+  const double er = wri[IPR] * igm1r +
+                    0.5 * wri[IDN] * (wri[IV1] * wri[IV1] + wri[IV2] * wri[IV2] + wri[IV3] * wri[IV3]);
+  const double rhoa = .5 * (wli[IDN] + wri[IDN]);
+  const double ca = .5 * (cl + cr);
+  const double pmid = .5 * (wli[IPR] + wri[IPR] + (wli[IV1] - wri[IV1]) * rhoa * ca);
+  double ql = 1.0, qr = 1.0;
+#if APH_EXACT
+  if (gt(pmid, wli[IPR])) ql = 1.0 + (gammal + 1) / sqrt(2 * gammal) * (pmid / wli[IPR] - 1.0);
+  if (gt(pmid, wri[IPR])) qr = 1.0 + (gammar + 1) / sqrt(2 * gammar) * (pmid / wri[IPR] - 1.0);
+#else
+  {
+    const bool bl = gt(pmid, wli[IPR]), br = gt(pmid, wri[IPR]);
+    if (bl || br) {
+      const double ipp = 1.0 / (wli[IPR] * wri[IPR]);  // shared reciprocal
+      const double kl = CONSTG ? gc.hlle_k : (gammal + 1) * rsqrt(2 * gammal);
+      const double kr = CONSTG ? gc.hlle_k : (gammar + 1) * rsqrt(2 * gammar);
+      if (bl) ql = fma(kl, fma(pmid * wri[IPR], ipp, -1.0), 1.0);
+      if (br) qr = fma(kr, fma(pmid * wli[IPR], ipp, -1.0), 1.0);
+    }
+  }
+#endif
+  const double al = wli[IV1] - cl * ql;
+  const double ar = wri[IV1] + cr * qr;
+  const double bp = is_pos(ar) ? ar : 0.0;
+  const double bm = is_neg(al) ? al : 0.0;
+  const double vxl = wli[IV1] - bm;
+  const double vxr = wri[IV1] - bp;
+  double fl[NHYDRO], fr[NHYDRO];
+  fl[IDN] = wli[IDN] * vxl;
+  fr[IDN] = wri[IDN] * vxr;
+  fl[IV1] = wli[IDN] * wli[IV1] * vxl;
+  fr[IV1] = wri[IDN] * wri[IV1] * vxr;
+  fl[IV2] = wli[IDN] * wli[IV2] * vxl;
+  fr[IV2] = wri[IDN] * wri[IV2] * vxr;
+  fl[IV3] = wli[IDN] * wli[IV3] * vxl;
+  fr[IV3] = wri[IDN] * wri[IV3] * vxr;
+  fl[IV1] += wli[IPR];
+  fr[IV1] += wri[IPR];
+  fl[IEN] = el * vxl + wli[IPR] * wli[IV1];
+  fr[IEN] = er * vxr + wri[IPR] * wri[IV1];
+  double tmp = 0.0;
+  if (__double_as_longlong(bp) != __double_as_longlong(bm) && (mag(bp) | mag(bm)) != 0ULL)
+    tmp = 0.5 * (bp + bm) / (bp - bm);
+#pragma unroll
+  for (int n = 0; n < NHYDRO; ++n) flxi[n] = 0.5 * (fl[n] + fr[n]) + (fl[n] - fr[n]) * tmp;
+}
+
+template <bool CONSTG, bool LOWMACH>
+__device__ __forceinline__ void solve_hllc(const double *wli, const double *wri, double glc,
+                                           double gle, double grc, double gre,
+                                           const GasConsts &gc, double *flxi) {
+  const double gammal = CONSTG ? gc.gamma : glc;
+  const double gammar = CONSTG ? gc.gamma : grc;
+  double igm1l, igm1r;
+  if (CONSTG) {
+    igm1l = igm1r = gc.igm1;
+  } else {
+    igm1l = 1.0 / (gle - 1);
+    igm1r = 1.0 / (gre - 1);
+  }
+  const double cl = sound_speed<CONSTG>(wli[IDN], wli[IPR], gammal, igm1l, gc);
+  const double cr = sound_speed<CONSTG>(wri[IDN], wri[IPR], gammar, igm1r, gc);
+  const double el = wli[IPR] * igm1l +
+                    0.5 * wli[IDN] * (wli[IV1] * wli[IV1] + wli[IV2] * wli[IV2] + wli[IV3] * wli[IV3]);
+  const double er = wri[IPR] * igm1r +
+                    0.5 * wri[IDN] * (wri[IV1] * wri[IV1] + wri[IV2] * wri[IV2] + wri[IV3] * wri[IV3]);
+  const double rhoa = .5 * (wli[IDN] + wri[IDN]);
+  const double ca = .5 * (cl + cr);
+  double pstar;
+  if (!LOWMACH) {
+    pstar = .5 * (wli[IPR] + wri[IPR]) - .5 * (wri[IV1] - wli[IV1]) * rhoa * ca;
+  } else {
+    // hydro_lhllc.hpp:71-79: "Mach" is the speed |v| itself
+    const double machl = sqrt(wli[IV1] * wli[IV1] + wli[IV2] * wli[IV2] + wli[IV3] * wli[IV3]);
+    const double machr = sqrt(wri[IV1] * wri[IV1] + wri[IV2] * wri[IV2] + wri[IV3] * wri[IV3]);
+    const double chi = smax(machl, machr);
+    const double phi = chi * (2.0 - chi);
+    pstar = .5 * (wli[IPR] + wri[IPR]) - .5 * (wri[IV1] - wli[IV1]) * rhoa * ca * phi;
+  }
+  double ql = 1.0, qr = 1.0;
+#if APH_EXACT
+  if (gt(pstar, wli[IPR])) ql = sqrt(1.0 + (gammal + 1) / (2 * gammar) * (pstar / wli[IPR] - 1.0));
+  if (gt(pstar, wri[IPR])) qr = sqrt(1.0 + (gammal + 1) / (2 * gammar) * (pstar / wri[IPR] - 1.0));
+#else
+  {
+    const bool bl = gt(pstar, wli[IPR]), br = gt(pstar, wri[IPR]);
+    if (bl || br) {
+      const double ipp = 1.0 / (wli[IPR] * wri[IPR]);
+      const double k = CONSTG ? gc.hllc_k : (gammal + 1) / (2 * gammar);
+      if (bl) ql = sqrt(fma(k, fma(pstar * wri[IPR], ipp, -1.0), 1.0));
+      if (br) qr = sqrt(fma(k, fma(pstar * wli[IPR], ipp, -1.0), 1.0));
+    }
+  }
+#endif
+  const double sl = wli[IV1] - cl * ql;
+  const double sr = wri[IV1] + cr * qr;
+  const double bp = is_pos(sr) ? sr : TINY_NUMBER;
+  const double bm = is_neg(sl) ? sl : -TINY_NUMBER;
+  double vxl = wli[IV1] - sl;
+  double vxr = wri[IV1] - sr;
+  const double tl = wli[IPR] + vxl * wli[IDN] * wli[IV1];
+  const double tr = wri[IPR] + vxr * wri[IDN] * wri[IV1];
+  const double ml = wli[IDN] * vxl;
+  const double mr = -(wri[IDN] * vxr);
+#if APH_EXACT
+  const double sstar = (tl - tr) / (ml + mr);
+  double cp = (ml * tr + mr * tl) / (ml + mr);
+#else
+  const double imm = 1.0 / (ml + mr);
+  const double sstar = (tl - tr) * imm;
+  double cp = (ml * tr + mr * tl) * imm;
+#endif
+  cp = is_pos(cp) ? cp : 0.0;
+  vxl = wli[IV1] - bm;
+  vxr = wri[IV1] - bp;
+  double fl[NHYDRO], fr[NHYDRO];
+  fl[IDN] = wli[IDN] * vxl;
+  fr[IDN] = wri[IDN] * vxr;
+  fl[IV1] = wli[IDN] * wli[IV1] * vxl + wli[IPR];
+  fr[IV1] = wri[IDN] * wri[IV1] * vxr + wri[IPR];
+  fl[IV2] = wli[IDN] * wli[IV2] * vxl;
+  fr[IV2] = wri[IDN] * wri[IV2] * vxr;
+  fl[IV3] = wli[IDN] * wli[IV3] * vxl;
+  fr[IV3] = wri[IDN] * wri[IV3] * vxr;
+  fl[IEN] = el * vxl + wli[IPR] * wli[IV1];
+  fr[IEN] = er * vxr + wri[IPR] * wri[IV1];
+  double ul, ur, ustar;
+  if (!is_neg(sstar)) {  // sstar >= 0.0
+#if APH_EXACT
+    ul = sstar / (sstar - bm);
+    ustar = -bm / (sstar - bm);
+#else
+    const double id = 1.0 / (sstar - bm);
+    ul = sstar * id;
+    ustar = -bm * id;
+#endif
+    ur = 0.0;
+  } else {
+#if APH_EXACT
+    ur = -sstar / (bp - sstar);
+    ustar = bp / (bp - sstar);
+#else
+    const double id = 1.0 / (bp - sstar);
+    ur = -sstar * id;
+    ustar = bp * id;
+#endif
+    ul = 0.0;
+  }
+  flxi[IDN] = ul * fl[IDN] + ur * fr[IDN];
+  flxi[IV1] = ul * fl[IV1] + ur * fr[IV1] + ustar * cp;
+  flxi[IV2] = ul * fl[IV2] + ur * fr[IV2];
+  flxi[IV3] = ul * fl[IV3] + ur * fr[IV3];
+  flxi[IEN] = ul * fl[IEN] + ur * fr[IEN] + ustar * cp * sstar;
+}
+
+template <int RS, bool CONSTG>
+__device__ __forceinline__ void riemann(const double *wl, const double *wr, double glc, double gle,
+                                        double grc, double gre, const GasConsts &gc,
+                                        double *flx) {
+  if (RS == RS_HLLE) {
+    solve_hlle<CONSTG>(wl, wr, glc, gle, grc, gre, gc, flx);
+  } else if (RS == RS_HLLC) {
+    solve_hllc<CONSTG, false>(wl, wr, glc, gle, grc, gre, gc, flx);
+  } else if (RS == RS_LHLLC) {
+    solve_hllc<CONSTG, true>(wl, wr, glc, gle, grc, gre, gc, flx);
+  } else {
+#pragma unroll
+    for (int n = 0; n < NHYDRO; ++n) flx[n] = 0.0;
+  }
+}
+
+}  // namespace aph

@@ -1,0 +1,136 @@
+/* aph_hydro.h -- C ABI of the GB300-native hydro flux path.
+ *
+ * The entry points replace the hydro package's device work in apophis: the
+ * "prim"/"gamma" FillDerived callback, the CalculateFluxes task, Parthenon's
+ * UpdateWithFluxDivergence and ApplyBoundaryConditions steps, the constant-g source
+ * and the EstimateTimestep callback.  Memory is owned by the caller (device
+ * pointers in plain structs), every call returns an aph_status, nothing throws,
+ * and each call is asynchronous on the given CUDA stream unless stated otherwise.
+ * Field layout is Parthenon's VariablePack: a meshblock field with nvar components
+ * is (nvar, nk, nj, ni) doubles, i fastest, with nghost ghost cells on both sides
+ * of every active dimension (nj = nk = 1 in 1D, nk = 1 in 2D).
+ */
+#ifndef APH_HYDRO_H_
+#define APH_HYDRO_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int aph_status;
+#define APH_OK 0
+#define APH_ERR_INVALID 1      /* bad argument: null pointer, size, enum, ghost width */
+#define APH_ERR_UNSUPPORTED 2  /* valid combination this build does not implement */
+#define APH_ERR_CUDA 3         /* a CUDA runtime call failed */
+#define APH_ERR_TIMEOUT 4      /* a bounded device-side wait gave up */
+#define APH_ERR_STATE 5        /* non-finite or non-positive density/pressure detected */
+
+/* Enumerations, numbered as src/main.hpp:32-53 */
+#define APH_RECON_DC 1
+#define APH_RECON_PLM 2
+#define APH_RECON_PPM 3
+#define APH_RSOLVER_NONE 1
+#define APH_RSOLVER_HLLE 2
+#define APH_RSOLVER_HLLC 3
+#define APH_RSOLVER_LHLLC 4
+#define APH_INTEGRATOR_RK1 1
+#define APH_INTEGRATOR_RK2 2
+#define APH_INTEGRATOR_RK3 3
+#define APH_INTEGRATOR_VL2 4
+/* Physical boundaries: Parthenon "periodic", "outflow" and apophis "reflecting"
+ * (src/boundaries/apophis_boundaries.cpp:257-272) */
+#define APH_BC_PERIODIC 0
+#define APH_BC_OUTFLOW 1
+#define APH_BC_REFLECT 2
+
+/* One meshblock (Parthenon MeshBlockData of the "base" and "u1" registers). */
+typedef struct aph_block {
+  double *cons;    /* "cons" (hydro.cpp:199-202), nvar components */
+  double *prim;    /* "prim" (hydro.cpp:223-225), nvar components */
+  double *gamma;   /* "gamma" (hydro.cpp:251-257): gamma_c, gamma_e */
+  double *u1;      /* "cons" of the u1 register (apophis_driver.cpp:45-54); may be NULL
+                      for calls that do not read it */
+  double *flux[3]; /* cons.flux(X1DIR..X3DIR), nvar components each, same shape as cons;
+                      flux[d] at (n,k,j,i) is the face on the low side of cell (k,j,i) */
+  int nx[3];       /* interior cells per dimension (1 for an unused dimension) */
+  double dx[3];    /* cell widths; for an unused dimension the mesh extent along it */
+} aph_block;
+
+/* Hydro package parameters (InitializeHydro, src/hydro/hydro.cpp:33-349). */
+typedef struct aph_hydro_params {
+  int ndim;        /* 1, 2 or 3 */
+  int nghost;      /* parthenon/mesh/nghost */
+  int nvar;        /* 5 + number of passive scalars */
+  int recon;       /* hydro/reconstruction */
+  int rsolver;     /* hydro/riemann */
+  double gm1;      /* eos/gm1 of the ideal gas */
+  double dfloor;   /* hydro/dfloor */
+  double pfloor;   /* hydro/pfloor */
+  double cfl;      /* parthenon/time/cfl */
+  int exact;       /* 1: the reference's operation order, one rounding per operation
+                      (bit-identical to its FP64 CPU path); 0: fused multiply-adds and
+                      shared reciprocals (about 1e-15 relative per operation) */
+} aph_hydro_params;
+
+/* A pack: the device-resident descriptor of a list of meshblocks (MeshData). */
+typedef struct aph_pack_s *aph_pack;
+
+/* Text of the last error on the calling thread ("" when none). */
+const char *aph_last_error(void);
+int aph_version(void);
+
+/* Describe nblocks meshblocks as one pack.  Uploads the descriptors to the device.
+ * Blocks may differ in nx; ndim, nghost and nvar are shared. */
+aph_status aph_pack_create(const aph_hydro_params *params, const aph_block *blocks, int nblocks,
+                           aph_pack *out);
+/* Blocks form a uniform nb[0] x nb[1] x nb[2] grid, numbered x-fastest, with the
+ * physical boundaries bc[2*d + side] (side 0 inner, 1 outer); needed by
+ * aph_hydro_fill_ghosts. */
+aph_status aph_pack_set_topology(aph_pack pack, const int nb[3], const int bc[6]);
+aph_status aph_pack_destroy(aph_pack pack);
+
+/* ConsToPrim<EOS_t> (src/hydro/hydro.cpp:422-533), the FillDerivedMesh callback:
+ * over the entire domain of each block, apply the density and pressure floors to
+ * cons in place and write prim and gamma. */
+aph_status aph_hydro_cons_to_prim(aph_pack pack, void *stream);
+
+/* CalculateFluxes<euler, recon, rsolver> (src/hydro/hydro.cpp:535-744), the
+ * flux_first_stage / flux_other_stage task (apophis_driver.cpp:70-72): reconstruct
+ * prim and gamma, solve the Riemann problem on every face of the interior and write
+ * cons.flux.  recon and rsolver are the template arguments of the FluxFun_t. */
+aph_status aph_hydro_calculate_fluxes(aph_pack pack, int recon, int rsolver, void *stream);
+
+/* Parthenon Update::UpdateWithFluxDivergence (called at apophis_driver.cpp:79-82):
+ * cons = gam0*cons + gam1*u1 + beta_dt*(-div F) on the interior.  The _dev variant
+ * takes beta_dt = beta * (*dt_dev) from device memory (for graph replay). */
+aph_status aph_hydro_update_with_flux_divergence(aph_pack pack, double gam0, double gam1,
+                                                 double beta_dt, void *stream);
+aph_status aph_hydro_update_with_flux_divergence_dev(aph_pack pack, double gam0, double gam1,
+                                                     double beta, const double *dt_dev,
+                                                     void *stream);
+
+/* EstimateTimestep<euler> (src/hydro/hydro.cpp:351-420), the EstimateTimestepMesh
+ * callback: cfl * min over interior cells of dx_d / (|v_d| + lambda).  The blocking
+ * form returns the value on the host; the _async form writes it to *dt_dev. */
+aph_status aph_hydro_estimate_timestep(aph_pack pack, double *dt_host, void *stream);
+aph_status aph_hydro_estimate_timestep_async(aph_pack pack, double *dt_dev, void *stream);
+
+/* ApplyGravity for a constant field g (src/gravity/gravity.cpp:374-410) with the
+ * stage's beta*dt; uses prim of the previous FillDerived as the reference does. */
+aph_status aph_hydro_apply_gravity(aph_pack pack, const double g[3], double beta_dt,
+                                   void *stream);
+
+/* Boundary exchange plus ApplyBoundaryConditions (apophis_driver.cpp:94-104) on a
+ * uniform block grid (aph_pack_set_topology): every ghost cell of cons takes the value
+ * of the interior cell its periodic / outflow / reflecting image points to; the
+ * reflecting image negates the normal momentum (apophis_boundaries.cpp:210-221). */
+aph_status aph_hydro_fill_ghosts(aph_pack pack, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* APH_HYDRO_H_ */

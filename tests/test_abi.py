@@ -1,0 +1,93 @@
+"""The C-ABI library: it builds, loads, exports every declared entry point, and rejects
+bad arguments with a status code and a message (no GPU needed: argument checks run
+before any CUDA call)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from apophis_gb300 import _capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+
+
+def declared_symbols():
+    names = set()
+    for fn in os.listdir(INCLUDE):
+        if fn.endswith(".h"):
+            src = open(os.path.join(INCLUDE, fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(aph_[a-z0-9_]+)\s*\(", src))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _capi.load()
+    names = declared_symbols()
+    assert "aph_hydro_calculate_fluxes" in names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the Python binding knows every one of them
+    known = set(_capi.SIGNATURES) | set(_capi.EXTRA_SIGNATURES)
+    assert not [n for n in names if n not in known]
+
+
+def _params(**kw):
+    base = dict(ndim=2, nghost=3, nvar=5, recon=3, rsolver=3, gm1=0.4, dfloor=1e-18,
+                pfloor=1e-18, cfl=0.3, exact=0)
+    base.update(kw)
+    return _capi.aph_hydro_params(*[base[f] for f, _ in _capi.aph_hydro_params._fields_])
+
+
+def _block():
+    b = _capi.aph_block()
+    b.cons = 0x1000  # never dereferenced: creation fails in validation first
+    b.nx[:] = [8, 8, 1]
+    b.dx[:] = [0.1, 0.1, 1.0]
+    return b
+
+
+@pytest.mark.parametrize("kw,needle", [
+    (dict(nghost=2, recon=3), "ghost"),
+    (dict(recon=7), "reconstruction"),
+    (dict(rsolver=9), "Riemann"),
+    (dict(rsolver=1, recon=2), "none"),
+    (dict(ndim=4), "ndim"),
+    (dict(gm1=-1.0), "gm1"),
+    (dict(nvar=3), "nvar"),
+])
+def test_pack_create_rejects_bad_params(kw, needle):
+    lib = _capi.load()
+    h = ctypes.c_void_p()
+    blk = (_capi.aph_block * 1)(_block())
+    st = lib.aph_pack_create(ctypes.byref(_params(**kw)), blk, 1, ctypes.byref(h))
+    assert st == 1  # APH_ERR_INVALID
+    assert needle in lib.aph_last_error().decode()
+    assert not h.value
+
+
+def test_pack_create_rejects_bad_blocks():
+    lib = _capi.load()
+    h = ctypes.c_void_p()
+    b = _block()
+    b.nx[2] = 4  # a third dimension in a 2D pack
+    st = lib.aph_pack_create(ctypes.byref(_params()), (_capi.aph_block * 1)(b), 1, ctypes.byref(h))
+    assert st == 1 and "nx3" in lib.aph_last_error().decode()
+    b = _block()
+    b.cons = None
+    st = lib.aph_pack_create(ctypes.byref(_params()), (_capi.aph_block * 1)(b), 1, ctypes.byref(h))
+    assert st == 1 and "cons" in lib.aph_last_error().decode()
+    st = lib.aph_pack_create(None, (_capi.aph_block * 1)(_block()), 1, ctypes.byref(h))
+    assert st == 1
+
+
+def test_null_pack_calls_fail_cleanly():
+    lib = _capi.load()
+    assert lib.aph_hydro_cons_to_prim(None, None) == 1
+    assert lib.aph_hydro_calculate_fluxes(None, 3, 3, None) == 1
+    assert lib.aph_hydro_fill_ghosts(None, None) == 1
+    d = ctypes.c_double()
+    assert lib.aph_hydro_estimate_timestep(None, ctypes.byref(d), None) == 1
+    assert lib.aph_pack_destroy(None) == 0
