@@ -30,6 +30,36 @@ class aph_hydro_params(ctypes.Structure):
                 ("cfl", ctypes.c_double), ("exact", ctypes.c_int)]
 
 
+class aph_stepper_desc(ctypes.Structure):
+    _fields_ = [("params", aph_hydro_params), ("integrator", ctypes.c_int),
+                ("nblocks", ctypes.c_int), ("blocks", ctypes.POINTER(aph_block)),
+                ("nb", ctypes.c_int * 3), ("bc", ctypes.c_int * 6),
+                ("use_gravity", ctypes.c_int), ("gravity", ctypes.c_double * 3),
+                ("tlim", ctypes.c_double), ("fixed_dt", ctypes.c_double)]
+
+
+class aph_stepper_config(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
+                ("lines", ctypes.c_int * 3), ("order", ctypes.c_int * 3),
+                ("schedule", ctypes.c_int), ("use_graph", ctypes.c_int)]
+
+    def to_dict(self):
+        return {"threads": self.threads, "ctas_per_sm": self.ctas_per_sm,
+                "lines": list(self.lines), "order": list(self.order),
+                "schedule": self.schedule, "use_graph": self.use_graph}
+
+    @classmethod
+    def from_dict(cls, d):
+        c = cls()
+        c.threads = d["threads"]
+        c.ctas_per_sm = d.get("ctas_per_sm", 0)
+        c.lines[:] = d["lines"]
+        c.order[:] = d["order"]
+        c.schedule = d["schedule"]
+        c.use_graph = d.get("use_graph", 1)
+        return c
+
+
 class AphError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), msg))
@@ -59,6 +89,19 @@ SIGNATURES = {
     "aph_hydro_apply_gravity": ([ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_void_p],
                                 ctypes.c_int),
     "aph_hydro_fill_ghosts": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_create": ([ctypes.POINTER(aph_stepper_desc), ctypes.POINTER(ctypes.c_void_p)],
+                           ctypes.c_int),
+    "aph_stepper_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_step": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_status": ([ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int),
+                            ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_get_config": ([ctypes.c_void_p, ctypes.POINTER(aph_stepper_config)],
+                               ctypes.c_int),
+    "aph_stepper_set_config": ([ctypes.c_void_p, ctypes.POINTER(aph_stepper_config)],
+                               ctypes.c_int),
+    "aph_stepper_profile": ([ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_autotune": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(aph_stepper_config),
+                              _dp], ctypes.c_int),
 }
 EXTRA_SIGNATURES = {}
 

@@ -30,11 +30,53 @@ struct PackDev {
   int mesh_nx[3];
 };
 
-// Work item of the fused stage kernel: one tile of one block.
-struct TileItem {
-  int block;
-  int t0[3];          // first interior cell of the tile
-  int tn[3];          // tile extent
+// ---- batched stepper -----------------------------------------------------------
+// One meshblock as the stepper sees it: the state u0 (caller-owned, ghosts included),
+// the stage-start copy u1, and stepper-owned scratch: prim and gamma of the stage input
+// (entire domain) and the accumulated flux difference du (interior only).
+struct StepBlock {
+  double *u0, *u1, *prim, *gamma, *du;
+  int nx[3];
+  int ni, nj, nk;
+  int loc[3];
+  long long ncell, nint;
+  double dx[3];
+};
+
+// Device-resident control block of a stepper (dt and time live on the device so that a
+// captured step replays without host round trips).
+struct StepCtl {
+  double dt;                    // dt of the next step
+  double time;
+  double tlim;                  // dt is clipped so that time never passes tlim
+  double dt_fixed;              // > 0: every step uses this dt
+  unsigned long long min_bits;  // dt reduction (bit pattern of the positive minimum)
+  int ncycle;
+  int error;                    // aph_status of a device-side failure (barrier timeout)
+  unsigned int bar_count, bar_gen;
+  unsigned int work[8];         // dynamic work counters, one per phase
+};
+
+// Arguments of one stage launch.
+struct StageArgs {
+  PackDev p;
+  const StepBlock *blocks;
+  StepCtl *ctl;
+  int *block_flags;             // per block: pressure floor applied somewhere in its cells
+  const int2 *cell_items;       // (block, first cell) chunks of blockDim.x entire-domain cells
+  int ncell_items;
+  const int2 *line_items[3];    // per direction: (block, first line) of T[d] lines
+  int nline_items[3];
+  int T[3];
+  int order[3];                 // sweep order (1-based directions)
+  double gam0, gam1, beta;
+  double grav[3];
+  int gravity;
+  int copy_u1;                  // stage 1: u1 <- u0 (interior, after the floors)
+  int last;                     // last stage: dt candidates of the new state
+  int init;                     // ghost fill + dt estimate only
+  int schedule;                 // 0 strided, 1 contiguous, 2 dynamic
+  unsigned long long timeout_ns;
 };
 
 }  // namespace aph
@@ -58,3 +100,14 @@ struct TileItem {
   }
 APH_DECLARE_LAUNCHERS(aph_fast)
 APH_DECLARE_LAUNCHERS(aph_exact)
+
+#define APH_DECLARE_STAGE(NS)                                                                  \
+  namespace NS {                                                                               \
+  size_t stage_smem_bytes(int recon, int n, int T);                                            \
+  const void *stage_kernel(int recon, int rsolver);                                            \
+  cudaError_t launch_stage(const aph::StageArgs &a, int recon, int rsolver, int grid,          \
+                           int threads, size_t smem, bool cooperative, cudaStream_t s);        \
+  cudaError_t stage_occupancy(int recon, int rsolver, int threads, size_t smem, int *blocks);  \
+  }
+APH_DECLARE_STAGE(aph_fast)
+APH_DECLARE_STAGE(aph_exact)

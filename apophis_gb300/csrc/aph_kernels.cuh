@@ -210,25 +210,6 @@ __global__ void __launch_bounds__(kThreads) k_update(PackDev p, const BlockDev *
 // atomic per CTA on the bit pattern (positive doubles order like unsigned integers,
 // NaN candidates sort above +inf and are ignored as fmin ignores them).
 // ---------------------------------------------------------------------------------------
-__device__ __forceinline__ double dt_candidate(const double *w, double e_cons, const double *dx,
-                                               int ndim, double gm1) {
-  const double e_internal =
-      (e_cons - 0.5 * w[IDN] * (w[IV1] * w[IV1] + w[IV2] * w[IV2] + w[IV3] * w[IV3])) / w[IDN];
-  const double bulkmod = eos_bulk_modulus(gm1, w[IDN], e_internal);
-  const double gamma_c = bulkmod / w[IPR];
-  const double lam = C_LIGHT * sqrt(gamma_c / (1 + (e_internal + C_LIGHT2) * w[IDN] / w[IPR]));
-  double m = dx[0] / (dabs(w[IV1]) + lam);
-  if (ndim > 1) {
-    const double c2 = dx[1] / (dabs(w[IV2]) + lam);
-    m = lt(c2, m) ? c2 : m;
-  }
-  if (ndim > 2) {
-    const double c3 = dx[2] / (dabs(w[IV3]) + lam);
-    m = lt(c3, m) ? c3 : m;
-  }
-  return m;
-}
-
 __device__ __forceinline__ unsigned long long block_min_bits(unsigned long long v) {
   __shared__ unsigned long long red[kThreads / 32];
 #pragma unroll

@@ -1,0 +1,553 @@
+// aph_stage.cuh -- the batched RK stage: one persistent launch per stage over every
+// meshblock of a pack, uneven block sizes included.
+//
+// Phases, separated by a grid-wide barrier whose waits are bounded in time:
+//   0  ghost zones of u0 from the neighbours' interiors and the physical boundaries
+//   1  ConsToPrim of u0 over the entire domain (floors applied to u0 in place, prim and
+//      gamma to scratch); at stage 1 the floored interior is copied to u1
+//   2+ one pass per direction: stage prim lines in shared memory, PPM with each face
+//      value computed once and shared by its two cells (or PLM / donor cell), Riemann
+//      solve, flux difference; the directions' differences accumulate in du in the
+//      reference's x, y, z order, and the last pass applies the RK update,
+//      the constant-g source and, at the last stage, the dt candidate of the new state.
+// Face states live in shared memory only.  On GB300 the FP64 pipe, not HBM, bounds this
+// kernel, so the design aims at the least FP64 work per zone: no reconstruction of
+// ghost rows, one evaluation per face value, constant adiabatic indices when no floor
+// fired, predicates on the integer pipe.
+#pragma once
+#include "aph_internal.h"
+#include "aph_math.cuh"
+
+#ifndef APH_NS
+#error "APH_NS must name the namespace of this translation unit"
+#endif
+
+namespace APH_NS {
+
+using namespace aph;
+
+constexpr int kStageThreads = 256;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid-wide barrier.  Every CTA of the launch is resident (the grid is sized from the
+// occupancy calculator, and launched cooperatively when possible); a wait that outlasts
+// timeout_ns records APH_ERR_TIMEOUT and the CTA leaves, so the launch always ends.
+__device__ __noinline__ bool grid_barrier(StepCtl *ctl, unsigned long long timeout_ns) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned int *vgen = &ctl->bar_gen;
+    volatile int *verr = &ctl->error;
+    const unsigned int gen = *vgen;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&ctl->bar_count, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch(&ctl->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&ctl->bar_gen, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (*vgen == gen) {
+        if (*verr) { ok = 0; break; }
+        __nanosleep(128);
+        if (global_ns() - t0 > timeout_ns) {
+          atomicCAS(&ctl->error, 0, 4 /* APH_ERR_TIMEOUT */);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Work distribution of a phase with n items.
+struct Sched {
+  int mode;
+  __device__ __forceinline__ int first(unsigned int *ctr, int n) const {
+    if (mode == 1) return (int)(((long long)blockIdx.x * n) / gridDim.x);
+    if (mode == 2) return next(ctr, n, -1);
+    return blockIdx.x;
+  }
+  __device__ __forceinline__ int next(unsigned int *ctr, int n, int cur) const {
+    if (mode == 1) {
+      const int end = (int)(((long long)(blockIdx.x + 1) * n) / gridDim.x);
+      return cur + 1 < end ? cur + 1 : n;
+    }
+    if (mode == 2) {
+      __shared__ int s_next;
+      __syncthreads();
+      if (threadIdx.x == 0) s_next = (int)atomicAdd(ctr, 1u);
+      __syncthreads();
+      return s_next < n ? s_next : n;
+    }
+    return cur + gridDim.x;
+  }
+};
+
+// ---- phase 0: ghost fill on a uniform block grid -------------------------------------
+__device__ __forceinline__ int map_index(int g, int n, int lo, int hi, bool &flip) {
+  if (g < 0) {
+    if (lo == 0) return g + n;      // periodic
+    if (lo == 1) return 0;          // outflow
+    flip = !flip;                   // reflecting
+    return -1 - g;
+  }
+  if (g >= n) {
+    if (hi == 0) return g - n;
+    if (hi == 1) return n - 1;
+    flip = !flip;
+    return 2 * n - 1 - g;
+  }
+  return g;
+}
+
+__device__ void ghost_cell(const StageArgs &a, const StepBlock &B, long long c) {
+  const PackDev &p = a.p;
+  const int idx[3] = {(int)(c % B.ni), (int)((c / B.ni) % B.nj), (int)(c / ((long long)B.ni * B.nj))};
+  bool ghost = false;
+  for (int d = 0; d < p.ndim; ++d) ghost |= (idx[d] < p.ng || idx[d] >= p.ng + B.nx[d]);
+  if (!ghost) return;
+  bool flip[3] = {false, false, false};
+  int sl[3], si[3];
+  for (int d = 0; d < 3; ++d) {
+    if (d < p.ndim) {
+      const int g = map_index(B.loc[d] * B.nx[d] + idx[d] - p.ng, p.mesh_nx[d], p.bc[d][0],
+                              p.bc[d][1], flip[d]);
+      sl[d] = g / B.nx[d];
+      si[d] = g - sl[d] * B.nx[d] + p.ng;
+    } else {
+      sl[d] = 0;
+      si[d] = 0;
+    }
+  }
+  const StepBlock &S = a.blocks[(sl[2] * p.nb[1] + sl[1]) * p.nb[0] + sl[0]];
+  const long long sc = ((long long)si[2] * S.nj + si[1]) * S.ni + si[0];
+#pragma unroll
+  for (int n = 0; n < NHYDRO; ++n) {
+    double v = S.u0[n * S.ncell + sc];
+    if ((n == IM1 && flip[0]) || (n == IM2 && flip[1]) || (n == IM3 && flip[2])) v = -v;
+    B.u0[n * B.ncell + c] = v;
+  }
+}
+
+__device__ __forceinline__ bool is_interior(const PackDev &p, const StepBlock &B, long long c,
+                                            int &i, int &j, int &k) {
+  i = (int)(c % B.ni);
+  j = (int)((c / B.ni) % B.nj);
+  k = (int)(c / ((long long)B.ni * B.nj));
+  bool in = i >= p.ng && i < p.ng + B.nx[0];
+  if (p.ndim >= 2) in = in && j >= p.ng && j < p.ng + B.nx[1];
+  if (p.ndim >= 3) in = in && k >= p.ng && k < p.ng + B.nx[2];
+  return in;
+}
+
+__device__ __forceinline__ unsigned long long block_min(unsigned long long v) {
+  __shared__ unsigned long long red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, v, o);
+    v = x < v ? x : v;
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : ~0ULL;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, v, o);
+      v = x < v ? x : v;
+    }
+  }
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long dt_bits(double m) {
+  return is_neg(m) ? ~0ULL : (unsigned long long)__double_as_longlong(m);
+}
+
+// ---- line geometry of a pass ----------------------------------------------------------
+// Line l of block B along DIR: the cell of interior position c on it is base + c*stride;
+// its interior index (for du) is ibase + c*istride.
+template <int DIR>
+__device__ __forceinline__ void line_of(const StepBlock &B, int ndim, int ng, int l,
+                                        long long &base, long long &stride, long long &ibase,
+                                        long long &istride) {
+  const int sj = ndim >= 2 ? ng : 0, sk = ndim >= 3 ? ng : 0;
+  const int n0 = B.nx[0], n1 = B.nx[1];
+  if (DIR == 1) {
+    const int j = l % n1, k = l / n1;
+    base = ((long long)(k + sk) * B.nj + (j + sj)) * B.ni + ng;
+    stride = 1;
+    ibase = (long long)l * n0;
+    istride = 1;
+  } else if (DIR == 2) {
+    const int i = l % n0, k = l / n0;
+    base = ((long long)(k + sk) * B.nj + sj) * B.ni + (i + ng);
+    stride = B.ni;
+    ibase = (long long)k * n1 * n0 + i;
+    istride = n0;
+  } else {
+    const int i = l % n0, j = l / n0;
+    base = ((long long)sk * B.nj + (j + sj)) * B.ni + (i + ng);
+    stride = (long long)B.ni * B.nj;
+    ibase = (long long)j * n0 + i;
+    istride = (long long)n0 * n1;
+  }
+}
+
+template <int RECON>
+struct Halo {
+  static constexpr int G = RECON == RECON_PPM ? 3 : RECON == RECON_PLM ? 2 : 1;
+};
+
+// Shared-memory doubles needed by one pass item of T lines of n cells with V
+// reconstructed variables.
+__host__ __device__ constexpr size_t pass_smem_doubles(int recon, int n, int T, int V) {
+  return recon == RECON_PPM
+             ? (size_t)V * T * ((n + 6) + 2 * (n + 4) + (n + 3) + (n + 2))
+             : (size_t)V * T * ((n + 2 * (recon == RECON_PLM ? 2 : 1)) + 2 * (n + 2));
+}
+
+// One pass item: lines l0..l0+nl-1 of block B along DIR.
+template <int DIR, int RECON, int RS>
+__device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl, int T,
+                          bool constg, bool first_pass, bool last_pass, double *sm,
+                          unsigned long long &dtmin) {
+  constexpr int G = Halo<RECON>::G;
+  const int n = B.nx[DIR - 1];
+  const int V = constg ? 5 : 7;
+  const int NW = n + 2 * G;
+  const long long nc = B.ncell;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  // shared-memory regions (V x T x width each)
+  double *W = sm;                                  // prim window, cells -G..n+G-1
+  double *D2 = W + (size_t)V * T * NW;             // PPM: d2, cells -2..n+1
+  double *DD = D2 + (RECON == RECON_PPM ? (size_t)V * T * (n + 4) : 0);  // PPM: dd
+  double *DPH = DD + (RECON == RECON_PPM ? (size_t)V * T * (n + 4) : 0);  // PPM: face values
+  double *SR = DPH + (RECON == RECON_PPM ? (size_t)V * T * (n + 3) : 0);  // right states
+  double *SL = (RECON == RECON_PPM) ? DD : SR + (size_t)V * T * (n + 2);  // left states
+  double *F = W;                                   // fluxes, after the window is dead
+  auto w_at = [&](int v, int t, int c) -> double & { return W[((size_t)v * T + t) * NW + c + G]; };
+
+  // A: load the window of prim (and gamma) along each line
+  {
+    const int per = nl * NW;
+    for (int it = tid; it < V * per; it += nth) {
+      const int v = it / per;
+      const int r = it - v * per;
+      int t, w;
+      if (DIR == 1) { t = r / NW; w = r - t * NW; } else { w = r / nl; t = r - w * nl; }
+      long long base, stride, ib, is;
+      line_of<DIR>(B, a.p.ndim, a.p.ng, l0 + t, base, stride, ib, is);
+      const double *src = v < NHYDRO ? B.prim + v * nc : B.gamma + (v - NHYDRO) * nc;
+      W[((size_t)v * T + t) * NW + w] = src[base + (long long)(w - G) * stride];
+    }
+  }
+  __syncthreads();
+  // B-D: reconstruction; left state of face c+1 -> SL[c+1], right state of face c -> SR[c+1]
+  if (RECON == RECON_PPM) {
+    const int w4 = n + 4, w3 = n + 3;
+    for (int it = tid; it < V * nl * w4; it += nth) {  // cells -2..n+1
+      const int v = it / (nl * w4);
+      const int r = it - v * nl * w4;
+      const int t = r / w4, c = r - t * w4 - 2;
+      const double qm = w_at(v, t, c - 1), q0 = w_at(v, t, c), qp = w_at(v, t, c + 1);
+      D2[((size_t)v * T + t) * w4 + c + 2] = ppm_d2(qm, q0, qp);
+      DD[((size_t)v * T + t) * w4 + c + 2] = ppm_dd(qm, q0, qp);
+    }
+    __syncthreads();
+    for (int it = tid; it < V * nl * w3; it += nth) {  // faces -1..n+1
+      const int v = it / (nl * w3);
+      const int r = it - v * nl * w3;
+      const int t = r / w3, f = r - t * w3 - 1;
+      const size_t o = ((size_t)v * T + t) * w4;
+      DPH[((size_t)v * T + t) * w3 + f + 1] =
+          ppm_face(w_at(v, t, f - 1), w_at(v, t, f), DD[o + f + 1], DD[o + f + 2], D2[o + f + 1],
+                   D2[o + f + 2]);
+    }
+    __syncthreads();
+    const int w2 = n + 2;
+    for (int it = tid; it < V * nl * w2; it += nth) {  // cells -1..n
+      const int v = it / (nl * w2);
+      const int r = it - v * nl * w2;
+      const int t = r / w2, c = r - t * w2 - 1;
+      const size_t o4 = ((size_t)v * T + t) * w4, o3 = ((size_t)v * T + t) * w3;
+      double ql, qr;
+      ppm_cell(w_at(v, t, c - 2), w_at(v, t, c - 1), w_at(v, t, c), w_at(v, t, c + 1),
+               w_at(v, t, c + 2), D2[o4 + c + 1], D2[o4 + c + 2], D2[o4 + c + 3], DPH[o3 + c + 1],
+               DPH[o3 + c + 2], ql, qr);
+      SL[((size_t)v * T + t) * w2 + c + 1] = ql;
+      SR[((size_t)v * T + t) * w2 + c + 1] = qr;
+    }
+  } else {
+    const int w2 = n + 2;
+    for (int it = tid; it < V * nl * w2; it += nth) {
+      const int v = it / (nl * w2);
+      const int r = it - v * nl * w2;
+      const int t = r / w2, c = r - t * w2 - 1;
+      double ql, qr;
+      if (RECON == RECON_PLM) {
+        plm(w_at(v, t, c - 1), w_at(v, t, c), w_at(v, t, c + 1), ql, qr);
+      } else {
+        ql = qr = w_at(v, t, c);
+      }
+      SL[((size_t)v * T + t) * w2 + c + 1] = ql;
+      SR[((size_t)v * T + t) * w2 + c + 1] = qr;
+    }
+  }
+  __syncthreads();
+  // E: Riemann solve on faces 0..n
+  {
+    constexpr int ivx = DIR;
+    constexpr int ivy = IV1 + ((ivx - IV1) + 1) % 3;
+    constexpr int ivz = IV1 + ((ivx - IV1) + 2) % 3;
+    const GasConsts gc{a.p.gm1, a.p.igm1, a.p.gamma, a.p.c2g, a.p.one_igm1, a.p.hlle_k, a.p.hllc_k};
+    const int w2 = n + 2, w1 = n + 1;
+    const size_t vs = (size_t)T * w2;
+    for (int it = tid; it < nl * w1; it += nth) {
+      const int t = it / w1, f = it - t * w1;
+      const size_t oL = (size_t)t * w2 + f, oR = oL + 1;
+      double wl[NHYDRO], wr[NHYDRO], flx[NHYDRO];
+      wl[IDN] = SL[IDN * vs + oL]; wl[IV1] = SL[ivx * vs + oL]; wl[IV2] = SL[ivy * vs + oL];
+      wl[IV3] = SL[ivz * vs + oL]; wl[IPR] = SL[IPR * vs + oL];
+      wr[IDN] = SR[IDN * vs + oR]; wr[IV1] = SR[ivx * vs + oR]; wr[IV2] = SR[ivy * vs + oR];
+      wr[IV3] = SR[ivz * vs + oR]; wr[IPR] = SR[IPR * vs + oR];
+#if APH_EXACT
+      riemann<RS, false>(wl, wr, SL[5 * vs + oL], SL[6 * vs + oL], SR[5 * vs + oR],
+                         SR[6 * vs + oR], gc, flx);
+#else
+      if (constg) {
+        riemann<RS, true>(wl, wr, 0.0, 0.0, 0.0, 0.0, gc, flx);
+      } else {
+        riemann<RS, false>(wl, wr, SL[5 * vs + oL], SL[6 * vs + oL], SR[5 * vs + oR],
+                           SR[6 * vs + oR], gc, flx);
+      }
+#endif
+      // store in cons order
+      const size_t fs = (size_t)T * w1;
+      const size_t of = (size_t)t * w1 + f;
+      F[IDN * fs + of] = flx[IDN];
+      F[ivx * fs + of] = flx[IV1];
+      F[ivy * fs + of] = flx[IV2];
+      F[ivz * fs + of] = flx[IV3];
+      F[IEN * fs + of] = flx[IEN];
+    }
+  }
+  __syncthreads();
+  // F: flux difference of each interior cell; du accumulates x, y, z in order
+  {
+    const int w1 = n + 1;
+    const size_t fs = (size_t)T * w1;
+    const double area = DIR == 1 ? B.dx[1] * B.dx[2] : DIR == 2 ? B.dx[0] * B.dx[2] : B.dx[0] * B.dx[1];
+    if (!last_pass) {
+      for (int it = tid; it < NHYDRO * nl * n; it += nth) {
+        const int v = it / (nl * n);
+        const int r = it - v * nl * n;
+        const int t = r / n, c = r - t * n;
+        long long base, stride, ib, is;
+        line_of<DIR>(B, a.p.ndim, a.p.ng, l0 + t, base, stride, ib, is);
+        const size_t of = v * fs + (size_t)t * w1 + c;
+        const double d = (area * F[of + 1] - area * F[of]);
+        double *du = B.du + v * B.nint + ib + c * is;
+        *du = first_pass ? d : *du + d;
+      }
+    } else {
+      const double vol = B.dx[0] * B.dx[1] * B.dx[2];
+      const double beta_dt = a.beta * a.ctl->dt;
+      for (int it = tid; it < nl * n; it += nth) {
+        const int t = it / n, c = it - t * n;
+        long long base, stride, ib, is;
+        line_of<DIR>(B, a.p.ndim, a.p.ng, l0 + t, base, stride, ib, is);
+        const long long cell = base + c * stride;
+        const long long icell = ib + c * is;
+        double u[NHYDRO];
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v) {
+          const size_t of = v * fs + (size_t)t * w1 + c;
+          double du = (area * F[of + 1] - area * F[of]);
+          if (!first_pass) du = B.du[v * B.nint + icell] + du;
+          const double div = -du / vol;
+          u[v] = a.gam0 * B.u0[v * nc + cell] + a.gam1 * B.u1[v * nc + cell] + beta_dt * div;
+        }
+        if (a.gravity) {  // ApplyGravity with the stage input's prim (gravity.cpp:386-407)
+          const double rho = B.prim[IDN * nc + cell];
+          u[IM1] += a.grav[0] * rho * beta_dt;
+          double de = a.grav[0] * B.prim[IV1 * nc + cell];
+          if (a.p.ndim >= 2) {
+            u[IM2] += a.grav[1] * rho * beta_dt;
+            de += a.grav[1] * B.prim[IV2 * nc + cell];
+          }
+          if (a.p.ndim >= 3) {
+            u[IM3] += a.grav[2] * rho * beta_dt;
+            de += a.grav[2] * B.prim[IV3 * nc + cell];
+          }
+          u[IEN] += de * rho * beta_dt;
+        }
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + cell] = u[v];
+        if (a.last) {  // EstimateTimestep on the floored new state
+          double w[NHYDRO], gcc, gce;
+          cons_to_prim_cell(u, w, gcc, gce, a.p.gm1, a.p.dfloor, a.p.pfloor);
+          const unsigned long long b = dt_bits(dt_candidate(w, u[IEN], B.dx, a.p.ndim, a.p.gm1));
+          dtmin = b < dtmin ? b : dtmin;
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <int RECON, int RS>
+__global__ void __launch_bounds__(kStageThreads, 1) k_stage(StageArgs a) {
+  extern __shared__ double sm[];
+  const PackDev &p = a.p;
+  const Sched sched{a.schedule};
+  unsigned long long dtmin = ~0ULL;
+  unsigned int *ctr = a.ctl->work;
+
+  // phase 0: ghost zones
+  for (int it = sched.first(ctr + 0, a.ncell_items); it < a.ncell_items;
+       it = sched.next(ctr + 0, a.ncell_items, it)) {
+    const int2 w = a.cell_items[it];
+    const StepBlock &B = a.blocks[w.x];
+    const long long c = (long long)w.y + threadIdx.x;
+    if (c < B.ncell) ghost_cell(a, B, c);
+  }
+  if (!a.init)
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < p.nblocks; b += gridDim.x * blockDim.x)
+      a.block_flags[b] = 0;
+  if (!grid_barrier(a.ctl, a.timeout_ns)) return;
+
+  // phase 1: ConsToPrim (in init mode only the dt estimate, nothing is written)
+  for (int it = sched.first(ctr + 1, a.ncell_items); it < a.ncell_items;
+       it = sched.next(ctr + 1, a.ncell_items, it)) {
+    const int2 w = a.cell_items[it];
+    const StepBlock &B = a.blocks[w.x];
+    const long long c = (long long)w.y + threadIdx.x;
+    if (c >= B.ncell) continue;
+    const long long nc = B.ncell;
+    double u[NHYDRO], wv[NHYDRO], g_c, g_e;
+#pragma unroll
+    for (int n = 0; n < NHYDRO; ++n) u[n] = B.u0[n * nc + c];
+    const double ud0 = u[IDN], ue0 = u[IEN];
+    const bool fl = cons_to_prim_cell(u, wv, g_c, g_e, p.gm1, p.dfloor, p.pfloor);
+    int i, j, k;
+    const bool inner = is_interior(p, B, c, i, j, k);
+    if (a.init) {
+      if (inner) {
+        const unsigned long long bb = dt_bits(dt_candidate(wv, u[IEN], B.dx, p.ndim, p.gm1));
+        dtmin = bb < dtmin ? bb : dtmin;
+      }
+      continue;
+    }
+    if (__double_as_longlong(u[IDN]) != __double_as_longlong(ud0)) B.u0[IDN * nc + c] = u[IDN];
+    if (__double_as_longlong(u[IEN]) != __double_as_longlong(ue0)) B.u0[IEN * nc + c] = u[IEN];
+#pragma unroll
+    for (int n = 0; n < NHYDRO; ++n) B.prim[n * nc + c] = wv[n];
+    B.gamma[c] = g_c;
+    B.gamma[nc + c] = g_e;
+    if (fl) atomicOr(&a.block_flags[w.x], 1);
+    if (a.copy_u1 && inner) {
+#pragma unroll
+      for (int n = 0; n < NHYDRO; ++n) B.u1[n * nc + c] = u[n];
+    }
+  }
+  if (a.init) {
+    dtmin = block_min(dtmin);
+    if (threadIdx.x == 0 && dtmin != ~0ULL) atomicMin(&a.ctl->min_bits, dtmin);
+    return;
+  }
+  if (!grid_barrier(a.ctl, a.timeout_ns)) return;
+
+  // phases 2..: one pass per direction
+  for (int pi = 0; pi < p.ndim; ++pi) {
+    const int dir = a.order[pi];
+    const int nit = a.nline_items[dir - 1];
+    const int T = a.T[dir - 1];
+    const bool first_pass = pi == 0, last_pass = pi == p.ndim - 1;
+    for (int it = sched.first(ctr + 2 + pi, nit); it < nit; it = sched.next(ctr + 2 + pi, nit, it)) {
+      const int2 w = a.line_items[dir - 1][it];
+      const StepBlock &B = a.blocks[w.x];
+      const int ntrans = dir == 1 ? B.nx[1] * B.nx[2] : dir == 2 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1];
+      const int nl = min(T, ntrans - w.y);
+#if APH_EXACT
+      const bool constg = false;
+#else
+      const bool constg = a.block_flags[w.x] == 0;
+#endif
+      if (dir == 1)
+        pass_item<1, RECON, RS>(a, B, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin);
+      else if (dir == 2)
+        pass_item<2, RECON, RS>(a, B, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin);
+      else
+        pass_item<3, RECON, RS>(a, B, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin);
+    }
+    if (!last_pass && !grid_barrier(a.ctl, a.timeout_ns)) return;
+  }
+  if (a.last) {
+    dtmin = block_min(dtmin);
+    if (threadIdx.x == 0 && dtmin != ~0ULL) atomicMin(&a.ctl->min_bits, dtmin);
+  }
+}
+
+// ---- host side ---------------------------------------------------------------------------
+size_t stage_smem_bytes(int recon, int n, int T) {
+  return pass_smem_doubles(recon, n, T, 7) * sizeof(double);
+}
+
+template <int RECON>
+static const void *kernel_for_rs(int rs) {
+  switch (rs) {
+    case RS_HLLE: return (const void *)k_stage<RECON, RS_HLLE>;
+    case RS_HLLC: return (const void *)k_stage<RECON, RS_HLLC>;
+    case RS_LHLLC: return (const void *)k_stage<RECON, RS_LHLLC>;
+    case RS_NONE: return RECON == RECON_DC ? (const void *)k_stage<RECON_DC, RS_NONE> : nullptr;
+    default: return nullptr;
+  }
+}
+
+const void *stage_kernel(int recon, int rsolver) {
+  if (recon == RECON_PPM) return kernel_for_rs<RECON_PPM>(rsolver);
+  if (recon == RECON_PLM) return kernel_for_rs<RECON_PLM>(rsolver);
+  if (recon == RECON_DC) return kernel_for_rs<RECON_DC>(rsolver);
+  return nullptr;
+}
+
+cudaError_t stage_occupancy(int recon, int rsolver, int threads, size_t smem, int *blocks) {
+  const void *k = stage_kernel(recon, rsolver);
+  if (!k) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, threads, smem);
+}
+
+cudaError_t launch_stage(const StageArgs &a, int recon, int rsolver, int grid, int threads,
+                         size_t smem, bool cooperative, cudaStream_t s) {
+  const void *k = stage_kernel(recon, rsolver);
+  if (!k) return cudaErrorInvalidValue;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = cooperative ? 1 : 0;
+  void *args[] = {(void *)&a};
+  return cudaLaunchKernelExC(&cfg, k, args);
+}
+
+}  // namespace APH_NS

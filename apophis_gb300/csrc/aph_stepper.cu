@@ -1,0 +1,690 @@
+// aph_stepper.cu -- the batched path: a whole RK step of a pack as persistent stage
+// launches, dt and time kept on the device, the step captured once as a CUDA graph and
+// replayed; plus the autotuner that picks CTA size, lines per work item, sweep order
+// and the CTA schedule.
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <vector>
+
+#include "../../include/aph_hydro.h"
+#include "aph_capi_internal.h"
+#include "aph_internal.h"
+
+using namespace aph;
+
+namespace {
+
+constexpr int kCellChunk = 256;
+
+__global__ void k_ctl_init(StepCtl *c, double tlim, double dt_fixed) {
+  c->dt = 0.0;
+  c->time = 0.0;
+  c->tlim = tlim;
+  c->dt_fixed = dt_fixed;
+  c->min_bits = ~0ULL;
+  c->ncycle = 0;
+  c->error = 0;
+  c->bar_count = 0;
+  c->bar_gen = 0;
+  for (int i = 0; i < 8; ++i) c->work[i] = 0;
+}
+
+__device__ __forceinline__ double min_to_dt(unsigned long long b, double cfl) {
+  const double m = (b == ~0ULL) ? DBL_MAX : __longlong_as_double((long long)b);
+  return cfl * m;
+}
+
+// After the initial estimate: dt_0 = cfl * min, clipped at tlim.
+__global__ void k_dt_initial(StepCtl *c, double cfl) {
+  double dt = c->dt_fixed > 0.0 ? c->dt_fixed : min_to_dt(c->min_bits, cfl);
+  if (c->dt_fixed <= 0.0 && c->time < c->tlim && (c->tlim - c->time) < dt) dt = c->tlim - c->time;
+  if (c->time >= c->tlim) dt = 0.0;
+  c->dt = dt;
+  c->min_bits = ~0ULL;
+}
+
+// End of a step: advance time, dt_{n+1} = min(2 dt_n, cfl * min), clipped at tlim.
+__global__ void k_dt_policy(StepCtl *c, double cfl) {
+  const double used = c->dt;
+  if (used > 0.0) {
+    c->time += used;
+    c->ncycle += 1;
+  }
+  double next;
+  if (c->dt_fixed > 0.0) {
+    next = c->time < c->tlim ? c->dt_fixed : 0.0;
+  } else {
+    const double est = min_to_dt(c->min_bits, cfl);
+    const double two = 2.0 * used;
+    next = (est < two) ? est : two;
+    if (c->time < c->tlim && (c->tlim - c->time) < next) next = c->tlim - c->time;
+    if (c->time >= c->tlim) next = 0.0;
+  }
+  c->dt = next;
+  c->min_bits = ~0ULL;
+  c->bar_count = 0;
+}
+
+struct Stage {
+  double gam0, gam1, beta;
+};
+
+std::vector<Stage> stages_of(int integrator) {
+  switch (integrator) {
+    case APH_INTEGRATOR_RK1: return {{0.0, 1.0, 1.0}};
+    case APH_INTEGRATOR_RK2: return {{0.0, 1.0, 1.0}, {0.5, 0.5, 0.5}};
+    case APH_INTEGRATOR_RK3:
+      return {{0.0, 1.0, 1.0}, {0.25, 0.75, 0.25}, {2.0 / 3.0, 1.0 / 3.0, 2.0 / 3.0}};
+    case APH_INTEGRATOR_VL2: return {{0.0, 1.0, 0.5}, {0.0, 1.0, 1.0}};
+    default: return {};
+  }
+}
+
+}  // namespace
+
+struct aph_stepper_s {
+  aph_hydro_params params;
+  int integrator = 0;
+  PackDev dev;
+  std::vector<StepBlock> hblocks;
+  StepBlock *d_blocks = nullptr;
+  double *d_u1 = nullptr, *d_prim = nullptr, *d_gamma = nullptr, *d_du = nullptr;
+  double *d_backup = nullptr;  // autotuner state backup
+  int *d_flags = nullptr;
+  StepCtl *d_ctl = nullptr;
+  int2 *d_cell_items = nullptr;
+  int ncell_items = 0;
+  int2 *d_line_items[3] = {nullptr, nullptr, nullptr};
+  int nline_items[3] = {0, 0, 0};
+  int T[3] = {0, 0, 0};
+  aph_stepper_config cfg;
+  int grid = 0;
+  size_t smem = 0;
+  bool cooperative = true;
+  double grav[3] = {0, 0, 0};
+  int gravity = 0;
+  long long total_cells = 0, total_interior = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cap = nullptr;
+  std::vector<std::vector<double *>> u0_ptrs;
+};
+
+namespace {
+
+aph_status upload_items(aph_stepper s, int2 **dst, const std::vector<int2> &v) {
+  if (*dst) cudaFree(*dst);
+  *dst = nullptr;
+  if (v.empty()) return APH_OK;
+  cudaError_t e = cudaMalloc(dst, v.size() * sizeof(int2));
+  if (e == cudaSuccess) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(int2), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "stepper items");
+}
+
+int auto_lines(int n) { return (n + 2 >= 256) ? 1 : std::max(1, 256 / (n + 2)); }
+
+void destroy_graph(aph_stepper s) {
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->exec = nullptr;
+  s->graph = nullptr;
+}
+
+// Build work lists, shared-memory size and grid for the current configuration.
+aph_status configure(aph_stepper s) {
+  destroy_graph(s);
+  const PackDev &p = s->dev;
+  const int nb = p.nblocks;
+  const int recon = s->params.recon;
+  // lines per item and shared memory per direction
+  size_t smem = 0;
+  for (int d = 0; d < p.ndim; ++d) {
+    const int n = p.max_nx[d];
+    int T = s->cfg.lines[d] > 0 ? s->cfg.lines[d] : auto_lines(n);
+    int ntr_max = 1;
+    for (const StepBlock &B : s->hblocks) {
+      const int ntr = d == 0 ? B.nx[1] * B.nx[2] : d == 1 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1];
+      ntr_max = std::max(ntr_max, ntr);
+    }
+    T = std::min(T, ntr_max);
+    s->T[d] = T;
+    const size_t need = s->params.exact ? aph_exact::stage_smem_bytes(recon, n, T)
+                                        : aph_fast::stage_smem_bytes(recon, n, T);
+    smem = std::max(smem, need);
+    std::vector<int2> items;
+    // schedule order: largest blocks first (longest-processing-time) so that the tail of a
+    // pass holds the small items
+    std::vector<int> order(nb);
+    for (int b = 0; b < nb; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      return s->hblocks[x].nint > s->hblocks[y].nint;
+    });
+    for (int b : order) {
+      const StepBlock &B = s->hblocks[b];
+      const int ntr = d == 0 ? B.nx[1] * B.nx[2] : d == 1 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1];
+      for (int l = 0; l < ntr; l += T) items.push_back(make_int2(b, l));
+    }
+    s->nline_items[d] = (int)items.size();
+    if (aph_status st = upload_items(s, &s->d_line_items[d], items)) return st;
+  }
+  if (smem > 220 * 1024)
+    return fail(APH_ERR_UNSUPPORTED, "stage needs %zu bytes of shared memory; use fewer lines", smem);
+  s->smem = smem;
+  const int threads = s->cfg.threads;
+  // every kernel instance a step launches (vl2's first stage reconstructs donor-cell)
+  std::vector<int> recons = {recon};
+  if (s->integrator == APH_INTEGRATOR_VL2 && recon != APH_RECON_DC) recons.push_back(APH_RECON_DC);
+  int per_sm = 1 << 30;
+  for (int rc : recons) {
+    int k = 0;
+    cudaError_t e = s->params.exact
+                        ? aph_exact::stage_occupancy(rc, s->params.rsolver, threads, smem, &k)
+                        : aph_fast::stage_occupancy(rc, s->params.rsolver, threads, smem, &k);
+    if (e != cudaSuccess) return cuda_fail(e, "stage occupancy");
+    per_sm = std::min(per_sm, k);
+  }
+  if (per_sm < 1) return fail(APH_ERR_UNSUPPORTED, "stage kernel does not fit on an SM");
+  if (s->cfg.ctas_per_sm > 0) per_sm = std::min(per_sm, s->cfg.ctas_per_sm);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  s->grid = per_sm * sms;
+  // entire-domain cell chunks
+  std::vector<int2> cells;
+  for (int b = 0; b < nb; ++b)
+    for (long long c = 0; c < s->hblocks[b].ncell; c += threads) cells.push_back(make_int2(b, (int)c));
+  s->ncell_items = (int)cells.size();
+  return upload_items(s, &s->d_cell_items, cells);
+}
+
+StageArgs stage_args(aph_stepper s, int stage_idx, const Stage &st, bool last, bool init) {
+  StageArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.p = s->dev;
+  a.blocks = s->d_blocks;
+  a.ctl = s->d_ctl;
+  a.block_flags = s->d_flags;
+  a.cell_items = s->d_cell_items;
+  a.ncell_items = s->ncell_items;
+  for (int d = 0; d < 3; ++d) {
+    a.line_items[d] = s->d_line_items[d];
+    a.nline_items[d] = s->nline_items[d];
+    a.T[d] = s->T[d];
+    a.order[d] = s->cfg.order[d];
+  }
+  a.gam0 = st.gam0;
+  a.gam1 = st.gam1;
+  a.beta = st.beta;
+  for (int d = 0; d < 3; ++d) a.grav[d] = s->grav[d];
+  a.gravity = s->gravity;
+  a.copy_u1 = stage_idx == 0;
+  a.last = last;
+  a.init = init;
+  a.schedule = s->cfg.schedule;
+  a.timeout_ns = 4000000000ULL;
+  return a;
+}
+
+cudaError_t launch_one(aph_stepper s, const StageArgs &a, int recon, cudaStream_t st) {
+  void *work = (char *)s->d_ctl + offsetof(StepCtl, work);
+  cudaError_t e = cudaMemsetAsync(work, 0, sizeof(((StepCtl *)nullptr)->work), st);
+  if (e != cudaSuccess) return e;
+  if (s->params.exact)
+    return aph_exact::launch_stage(a, recon, s->params.rsolver, s->grid, s->cfg.threads, s->smem,
+                                   s->cooperative, st);
+  return aph_fast::launch_stage(a, recon, s->params.rsolver, s->grid, s->cfg.threads, s->smem,
+                                s->cooperative, st);
+}
+
+// Enqueue one full RK step (all stages + dt policy).
+cudaError_t enqueue_step(aph_stepper s, cudaStream_t st) {
+  const std::vector<Stage> stages = stages_of(s->integrator);
+  for (size_t i = 0; i < stages.size(); ++i) {
+    const bool last = i + 1 == stages.size();
+    const int recon = (s->integrator == APH_INTEGRATOR_VL2 && i == 0) ? APH_RECON_DC : s->params.recon;
+    StageArgs a = stage_args(s, (int)i, stages[i], last, false);
+    cudaError_t e = launch_one(s, a, recon, st);
+    if (e != cudaSuccess) return e;
+  }
+  k_dt_policy<<<1, 1, 0, st>>>(s->d_ctl, s->dev.cfl);
+  return cudaGetLastError();
+}
+
+aph_status build_graph(aph_stepper s) {
+  destroy_graph(s);
+  if (!s->cap) {
+    cudaError_t e = cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "capture stream");
+  }
+  for (int attempt = 0;; ++attempt) {
+    cudaError_t e = cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+    cudaError_t e2 = enqueue_step(s, s->cap);
+    e = cudaStreamEndCapture(s->cap, &s->graph);
+    if (e2 == cudaSuccess && e == cudaSuccess) break;
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->graph = nullptr;
+    cudaGetLastError();
+    // a cooperative launch that cannot be captured: capture a plain launch of the same
+    // occupancy-sized grid (its barrier waits stay bounded)
+    if (s->cooperative && attempt == 0) {
+      s->cooperative = false;
+      continue;
+    }
+    return cuda_fail(e2 != cudaSuccess ? e2 : e, "capture step");
+  }
+  cudaError_t e;
+  e = cudaGraphInstantiate(&s->exec, s->graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(s->graph);
+    s->graph = nullptr;
+    return cuda_fail(e, "instantiate step graph");
+  }
+  return APH_OK;
+}
+
+aph_status initial_dt(aph_stepper s, cudaStream_t st) {
+  StageArgs a = stage_args(s, 0, Stage{0, 1, 1}, false, true);
+  cudaError_t e = launch_one(s, a, s->params.recon, st);
+  if (e == cudaSuccess) {
+    k_dt_initial<<<1, 1, 0, st>>>(s->d_ctl, s->dev.cfl);
+    e = cudaGetLastError();
+  }
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "initial dt");
+}
+
+aph_status read_ctl(aph_stepper s, StepCtl *out) {
+  cudaError_t e = cudaMemcpy(out, s->d_ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "read stepper state");
+  if (out->error) return fail(out->error, "device-side failure in the stage kernel (status %d)", out->error);
+  return APH_OK;
+}
+
+void free_all(aph_stepper s) {
+  destroy_graph(s);
+  if (s->cap) cudaStreamDestroy(s->cap);
+  cudaFree(s->d_blocks);
+  cudaFree(s->d_u1);
+  cudaFree(s->d_prim);
+  cudaFree(s->d_gamma);
+  cudaFree(s->d_du);
+  cudaFree(s->d_backup);
+  cudaFree(s->d_flags);
+  cudaFree(s->d_ctl);
+  cudaFree(s->d_cell_items);
+  for (int d = 0; d < 3; ++d) cudaFree(s->d_line_items[d]);
+}
+
+}  // namespace
+
+extern "C" {
+
+aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
+  clear_error();
+  if (!desc || !out) return fail(APH_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (aph_status st = validate_params(&desc->params)) return st;
+  if (desc->params.nvar != 5)
+    return fail(APH_ERR_UNSUPPORTED, "the batched stepper carries no passive scalars (nvar 5)");
+  if (stages_of(desc->integrator).empty())
+    return fail(APH_ERR_INVALID, "integrator %d not recognized", desc->integrator);
+  if (desc->nblocks <= 0 || !desc->blocks) return fail(APH_ERR_INVALID, "no blocks");
+  const int ndim = desc->params.ndim;
+  if ((long long)desc->nb[0] * desc->nb[1] * desc->nb[2] != desc->nblocks)
+    return fail(APH_ERR_INVALID, "nb product != nblocks");
+  aph_stepper s = new aph_stepper_s();
+  s->params = desc->params;
+  s->integrator = desc->integrator;
+  PackDev &p = s->dev;
+  std::memset(&p, 0, sizeof(p));
+  p.nblocks = desc->nblocks;
+  p.ndim = ndim;
+  p.ng = desc->params.nghost;
+  p.nvar = 5;
+  p.gm1 = desc->params.gm1;
+  p.dfloor = desc->params.dfloor;
+  p.pfloor = desc->params.pfloor;
+  p.cfl = desc->params.cfl;
+  fill_gas_consts(p);
+  for (int d = 0; d < 3; ++d) {
+    if (d >= ndim && desc->nb[d] != 1) {
+      delete s;
+      return fail(APH_ERR_INVALID, "nb%d must be 1", d + 1);
+    }
+    p.nb[d] = desc->nb[d];
+    p.bc[d][0] = desc->bc[2 * d];
+    p.bc[d][1] = desc->bc[2 * d + 1];
+    for (int k = 0; k < 2; ++k)
+      if (p.bc[d][k] < APH_BC_PERIODIC || p.bc[d][k] > APH_BC_REFLECT) {
+        delete s;
+        return fail(APH_ERR_INVALID, "bc not recognized");
+      }
+  }
+  s->hblocks.resize(p.nblocks);
+  long long cells = 0, inter = 0;
+  for (int b = 0; b < p.nblocks; ++b) {
+    const aph_block &a = desc->blocks[b];
+    StepBlock &B = s->hblocks[b];
+    std::memset(&B, 0, sizeof(B));
+    for (int d = 0; d < 3; ++d) {
+      if (d < ndim ? a.nx[d] < 1 : a.nx[d] != 1) {
+        delete s;
+        return fail(APH_ERR_INVALID, "block %d: nx%d invalid", b, d + 1);
+      }
+      if (a.nx[d] != desc->blocks[0].nx[d]) {
+        delete s;
+        return fail(APH_ERR_UNSUPPORTED, "a block grid with ghost exchange needs equal blocks");
+      }
+      if (!(a.dx[d] > 0.0)) {
+        delete s;
+        return fail(APH_ERR_INVALID, "block %d: dx%d must be positive", b, d + 1);
+      }
+      B.nx[d] = a.nx[d];
+      B.dx[d] = a.dx[d];
+      p.max_nx[d] = std::max(p.max_nx[d], a.nx[d]);
+    }
+    if (!a.cons) {
+      delete s;
+      return fail(APH_ERR_INVALID, "block %d: cons is NULL", b);
+    }
+    B.u0 = a.cons;
+    B.ni = a.nx[0] + 2 * p.ng;
+    B.nj = ndim >= 2 ? a.nx[1] + 2 * p.ng : 1;
+    B.nk = ndim >= 3 ? a.nx[2] + 2 * p.ng : 1;
+    B.ncell = (long long)B.ni * B.nj * B.nk;
+    B.nint = (long long)a.nx[0] * a.nx[1] * a.nx[2];
+    B.loc[0] = b % p.nb[0];
+    B.loc[1] = (b / p.nb[0]) % p.nb[1];
+    B.loc[2] = b / (p.nb[0] * p.nb[1]);
+    cells += B.ncell;
+    inter += B.nint;
+  }
+  for (int d = 0; d < 3; ++d) p.mesh_nx[d] = p.nb[d] * s->hblocks[0].nx[d];
+  s->total_cells = cells;
+  s->total_interior = inter;
+  s->gravity = desc->use_gravity != 0;
+  for (int d = 0; d < 3; ++d) s->grav[d] = desc->gravity[d];
+  s->cfg.threads = 256;
+  s->cfg.ctas_per_sm = 0;
+  for (int d = 0; d < 3; ++d) {
+    s->cfg.lines[d] = 0;
+    s->cfg.order[d] = d + 1;
+  }
+  s->cfg.schedule = 0;
+  s->cfg.use_graph = 1;
+  cudaError_t e = cudaSuccess;
+  auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+  ck(cudaMalloc(&s->d_u1, sizeof(double) * 5 * cells));
+  ck(cudaMalloc(&s->d_prim, sizeof(double) * 5 * cells));
+  ck(cudaMalloc(&s->d_gamma, sizeof(double) * 2 * cells));
+  ck(cudaMalloc(&s->d_du, sizeof(double) * 5 * inter));
+  ck(cudaMalloc(&s->d_flags, sizeof(int) * p.nblocks));
+  ck(cudaMalloc(&s->d_ctl, sizeof(StepCtl)));
+  ck(cudaMalloc(&s->d_blocks, sizeof(StepBlock) * p.nblocks));
+  if (e != cudaSuccess) {
+    free_all(s);
+    delete s;
+    return cuda_fail(e, "stepper allocation");
+  }
+  long long oc = 0, oi = 0;
+  for (int b = 0; b < p.nblocks; ++b) {
+    StepBlock &B = s->hblocks[b];
+    B.u1 = s->d_u1 + 5 * oc;
+    B.prim = s->d_prim + 5 * oc;
+    B.gamma = s->d_gamma + 2 * oc;
+    B.du = s->d_du + 5 * oi;
+    oc += B.ncell;
+    oi += B.nint;
+  }
+  ck(cudaMemcpy(s->d_blocks, s->hblocks.data(), sizeof(StepBlock) * p.nblocks, cudaMemcpyHostToDevice));
+  ck(cudaMemset(s->d_flags, 0, sizeof(int) * p.nblocks));
+  k_ctl_init<<<1, 1>>>(s->d_ctl, desc->tlim > 0 ? desc->tlim : DBL_MAX, desc->fixed_dt);
+  ck(cudaGetLastError());
+  if (e != cudaSuccess) {
+    free_all(s);
+    delete s;
+    return cuda_fail(e, "stepper setup");
+  }
+  if (aph_status st = configure(s)) {
+    free_all(s);
+    delete s;
+    return st;
+  }
+  aph_status st = initial_dt(s, 0);
+  if (st == APH_OK) {
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) st = cuda_fail(e, "initial dt");
+  }
+  if (st == APH_OK) {
+    StepCtl c;
+    st = read_ctl(s, &c);
+  }
+  if (st) {
+    free_all(s);
+    delete s;
+    return st;
+  }
+  *out = s;
+  return APH_OK;
+}
+
+aph_status aph_stepper_destroy(aph_stepper s) {
+  if (!s) return APH_OK;
+  free_all(s);
+  delete s;
+  return APH_OK;
+}
+
+aph_status aph_stepper_step(aph_stepper s, int nsteps, void *stream) {
+  clear_error();
+  if (!s) return fail(APH_ERR_INVALID, "stepper is NULL");
+  if (nsteps < 0) return fail(APH_ERR_INVALID, "nsteps < 0");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (s->cfg.use_graph) {
+    if (!s->exec) {
+      if (aph_status r = build_graph(s)) return r;
+    }
+    for (int i = 0; i < nsteps; ++i) {
+      cudaError_t e = cudaGraphLaunch(s->exec, st);
+      if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+    }
+    return APH_OK;
+  }
+  for (int i = 0; i < nsteps; ++i) {
+    cudaError_t e = enqueue_step(s, st);
+    if (e != cudaSuccess) return cuda_fail(e, "stage launch");
+  }
+  return APH_OK;
+}
+
+aph_status aph_stepper_status(aph_stepper s, double *time, double *dt, int *ncycle, void *stream) {
+  clear_error();
+  if (!s) return fail(APH_ERR_INVALID, "stepper is NULL");
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "stepper status");
+  StepCtl c;
+  aph_status st = read_ctl(s, &c);
+  if (time) *time = c.time;
+  if (dt) *dt = c.dt;
+  if (ncycle) *ncycle = c.ncycle;
+  return st;
+}
+
+aph_status aph_stepper_get_config(aph_stepper s, aph_stepper_config *cfg) {
+  clear_error();
+  if (!s || !cfg) return fail(APH_ERR_INVALID, "NULL argument");
+  *cfg = s->cfg;
+  for (int d = 0; d < 3; ++d) cfg->lines[d] = d < s->dev.ndim ? s->T[d] : 0;
+  return APH_OK;
+}
+
+aph_status aph_stepper_set_config(aph_stepper s, const aph_stepper_config *cfg) {
+  clear_error();
+  if (!s || !cfg) return fail(APH_ERR_INVALID, "NULL argument");
+  if (cfg->threads < 64 || cfg->threads > 1024 || cfg->threads % 32)
+    return fail(APH_ERR_INVALID, "threads must be a multiple of 32 in 64..1024");
+  if (cfg->threads > 256) return fail(APH_ERR_UNSUPPORTED, "stage kernel is built for <= 256 threads");
+  if (cfg->schedule < 0 || cfg->schedule > 2) return fail(APH_ERR_INVALID, "schedule not in 0..2");
+  int seen = 0;
+  for (int d = 0; d < s->dev.ndim; ++d) {
+    if (cfg->order[d] < 1 || cfg->order[d] > s->dev.ndim) return fail(APH_ERR_INVALID, "bad sweep order");
+    seen |= 1 << cfg->order[d];
+  }
+  if (seen != ((1 << (s->dev.ndim + 1)) - 2)) return fail(APH_ERR_INVALID, "sweep order is not a permutation");
+  if (s->params.exact)
+    for (int d = 0; d < s->dev.ndim; ++d)
+      if (cfg->order[d] != d + 1)
+        return fail(APH_ERR_INVALID, "exact mode sums the directions in x, y, z order");
+  aph_stepper_config old = s->cfg;
+  s->cfg = *cfg;
+  for (int d = s->dev.ndim; d < 3; ++d) s->cfg.order[d] = d + 1;
+  if (aph_status st = configure(s)) {
+    s->cfg = old;
+    configure(s);
+    return st;
+  }
+  return APH_OK;
+}
+
+// Run nsteps steps without the graph, timing every stage launch with CUDA events on the
+// launching stream; stage_ms[i] gets the mean duration of stage i.
+aph_status aph_stepper_profile(aph_stepper s, int nsteps, double *stage_ms, void *stream) {
+  clear_error();
+  if (!s || !stage_ms || nsteps < 1) return fail(APH_ERR_INVALID, "bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const std::vector<Stage> stages = stages_of(s->integrator);
+  const int ns = (int)stages.size();
+  std::vector<cudaEvent_t> ev(2 * ns * nsteps);
+  for (auto &e : ev) cudaEventCreate(&e);
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < nsteps && e == cudaSuccess; ++k) {
+    for (int i = 0; i < ns && e == cudaSuccess; ++i) {
+      const bool last = i + 1 == ns;
+      const int recon = (s->integrator == APH_INTEGRATOR_VL2 && i == 0) ? APH_RECON_DC : s->params.recon;
+      StageArgs a = stage_args(s, i, stages[i], last, false);
+      void *work = (char *)s->d_ctl + offsetof(StepCtl, work);
+      e = cudaMemsetAsync(work, 0, sizeof(((StepCtl *)nullptr)->work), st);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[2 * (k * ns + i)], st);
+      if (e == cudaSuccess)
+        e = s->params.exact ? aph_exact::launch_stage(a, recon, s->params.rsolver, s->grid, s->cfg.threads,
+                                                      s->smem, s->cooperative, st)
+                            : aph_fast::launch_stage(a, recon, s->params.rsolver, s->grid, s->cfg.threads,
+                                                     s->smem, s->cooperative, st);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[2 * (k * ns + i) + 1], st);
+    }
+    if (e == cudaSuccess) {
+      k_dt_policy<<<1, 1, 0, st>>>(s->d_ctl, s->dev.cfl);
+      e = cudaGetLastError();
+    }
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  for (int i = 0; i < ns; ++i) stage_ms[i] = 0.0;
+  if (e == cudaSuccess)
+    for (int k = 0; k < nsteps; ++k)
+      for (int i = 0; i < ns; ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[2 * (k * ns + i)], ev[2 * (k * ns + i) + 1]);
+        stage_ms[i] += ms / nsteps;
+      }
+  for (auto &x : ev) cudaEventDestroy(x);
+  if (e != cudaSuccess) return cuda_fail(e, "stepper profile");
+  StepCtl c;
+  return read_ctl(s, &c);
+}
+
+// Time candidate configurations on a scratch copy of the state and keep the fastest.
+aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_config *best,
+                                double *best_ms) {
+  clear_error();
+  if (!s) return fail(APH_ERR_INVALID, "stepper is NULL");
+  if (trial_steps < 1) trial_steps = 2;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "autotune");
+  // back up u0 of every block and the control block
+  const size_t nb5 = sizeof(double) * 5;
+  if (!s->d_backup) {
+    e = cudaMalloc(&s->d_backup, nb5 * s->total_cells);
+    if (e != cudaSuccess) return cuda_fail(e, "autotune backup");
+  }
+  StepCtl ctl_saved;
+  e = cudaMemcpy(&ctl_saved, s->d_ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost);
+  long long off = 0;
+  for (const StepBlock &B : s->hblocks) {
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_backup + 5 * off, B.u0, nb5 * B.ncell, cudaMemcpyDeviceToDevice);
+    off += B.ncell;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "autotune backup");
+  auto restore = [&]() {
+    long long o = 0;
+    for (const StepBlock &B : s->hblocks) {
+      cudaMemcpy(B.u0, s->d_backup + 5 * o, nb5 * B.ncell, cudaMemcpyDeviceToDevice);
+      o += B.ncell;
+    }
+    cudaMemcpy(s->d_ctl, &ctl_saved, sizeof(StepCtl), cudaMemcpyHostToDevice);
+  };
+  // candidate set
+  std::vector<aph_stepper_config> cands;
+  const aph_stepper_config base = s->cfg;
+  const int ndim = s->dev.ndim;
+  std::vector<std::vector<int>> orders = {{1, 2, 3}};
+  if (!s->params.exact && ndim == 2) orders.push_back({2, 1, 3});
+  if (!s->params.exact && ndim == 3) {
+    orders.push_back({3, 2, 1});
+    orders.push_back({2, 3, 1});
+  }
+  for (int threads : {128, 256})
+    for (int lscale : {1, 2})
+      for (int sched : {0, 1, 2})
+        for (const auto &o : orders) {
+          aph_stepper_config c = base;
+          c.threads = threads;
+          c.schedule = sched;
+          c.ctas_per_sm = 0;
+          c.use_graph = 1;
+          for (int d = 0; d < 3; ++d) {
+            c.order[d] = o[d];
+            const int n = s->dev.max_nx[d];
+            const int auto_l = (n + 2 >= threads) ? 1 : std::max(1, threads / (n + 2));
+            c.lines[d] = std::max(1, auto_l * lscale);
+          }
+          cands.push_back(c);
+        }
+  double best_t = 1e300;
+  aph_stepper_config best_c = base;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (const aph_stepper_config &c : cands) {
+    if (aph_stepper_set_config(s, &c) != APH_OK) continue;
+    restore();
+    if (aph_stepper_step(s, 1, 0) != APH_OK) continue;  // warm-up (and graph build)
+    cudaEventRecord(e0, 0);
+    if (aph_stepper_step(s, trial_steps, 0) != APH_OK) continue;
+    cudaEventRecord(e1, 0);
+    cudaEventSynchronize(e1);
+    StepCtl c2;
+    if (read_ctl(s, &c2) != APH_OK) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double per = ms / trial_steps;
+    if (per < best_t) {
+      best_t = per;
+      best_c = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  aph_status st = aph_stepper_set_config(s, &best_c);
+  restore();
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "autotune");
+  if (best) aph_stepper_get_config(s, best);
+  if (best_ms) *best_ms = best_t;
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,291 @@
+"""Benchmark of the hydro flux path on one GB300.
+
+Headline workload (the BASELINE configuration that fits one GPU): 3D Kelvin-Helmholtz,
+256^3 periodic unit box as 64 meshblocks of 64^3 with 4 ghost cells, PPM + HLLC, RK2,
+CFL 0.3, gamma 5/3, FP64, synthetic initial data.  A "step" is one full RK2 step of the
+whole pack (2 stages + the CFL dt reduction).
+
+value   zone-updates/s of the batched path (one persistent launch per stage over all 64
+        meshblocks, the step replayed as a CUDA graph), state resident in HBM.
+e2e     the same through the C ABI with the state in pinned host memory: every step
+        copies cons host->device, steps, copies cons device->host.
+plain   the per-meshblock launch path (one launch per kernel per meshblock).
+roofline  HBM roofline of the stage kernel with the algorithmic 200 B per zone-update
+        (stage 1: read U^n, write U^1; stage 2: read U^1 and U^n, write U^n+1), and the
+        FP64-pipe roofline that actually binds it.
+cpu_baseline  the oracle (C++ FP64 restatement of the reference's CPU path) on the host
+        cores, a bounded sample of the same workload.
+
+--impl reference times that CPU path alone (all host threads) on the same workload.
+Under torchrun (N > 1) every rank runs its own replica of the workload (the hydro step
+shards by meshblocks, but this build drives one GPU per replica and exchanges nothing);
+the step time is the max over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "zone-updates/s (PPM+HLLC, FP64) batched vs plain; adjoint/forward time ratio"
+UNIT = "zone-updates/s"
+WORKLOAD = ("kh3d 256^3: 64 meshblocks of 64^3, 4 ghost cells, PPM+HLLC, RK2, CFL 0.3, "
+            "gamma 5/3, FP64")
+BYTES_PER_ZONE_UPDATE = 200.0   # RK2 with 5 FP64 conserved variables
+# FP64 instructions per zone-update of the stage kernel (fast mode), from the ncu
+# capture summarised in profiles/stage_kernel_kh3d.md (sm__inst_executed_pipe_fp64 per
+# zone-update; one warp instruction = 32 lane operations)
+FP64_LANE_OPS_PER_ZONE_UPDATE = None
+FP64_LANES_PER_CLK_PER_SM = 2.05   # measured DFMA rate on GB300 (profiles/fp64_pipe_gb300.md)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured", d
+    return 6800.0, "fallback", {}
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = "/tmp/aph_clocks_%d.csv" % os.getpid()
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("APH_BENCH_BACKEND") != "gloo" else "gloo")
+        return dist, rank, ws
+    return None, 0, 1
+
+
+def cpu_baseline(cfg, cons, nsteps, threads=None):
+    """Oracle (C++ FP64 restatement of the reference path) on the host cores."""
+    from oracle import oracle as O
+    if threads:
+        O.set_num_threads(threads)
+    m = O.Mesh(cfg)
+    m.set_cons(cons)
+    m.run(nsteps=1)  # warm-up
+    t0 = time.perf_counter()
+    m.run(nsteps=nsteps)
+    el = time.perf_counter() - t0
+    return cfg.zones() * nsteps / el, O.num_threads(), el
+
+
+def run_reference(args, cfg, cons):
+    dist, rank, ws = dist_init()
+    if rank != 0:
+        return
+    nsteps = max(1, min(args.steps, 2))
+    zps, cores, el = cpu_baseline(cfg, cons, nsteps)
+    line = {"impl": "reference", "metric": METRIC, "value": zps, "unit": UNIT, "n_gpus": ws,
+            "steps": nsteps, "warmup": 1, "ms_per_step": el / nsteps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "parallelism": "host threads"},
+            "cpu_baseline": {"value": zps, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d full RK2 steps of the 256^3 pack after 1 warm-up" % nsteps},
+            "e2e": {"value": zps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="mesh cells per side")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the per-meshblock path")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    from apophis_gb300 import problems
+    cfg, cons = problems.kh3d(n=args.n, block=64 if args.n >= 64 else args.n // 2, ng=4)
+    if args.impl == "reference":
+        run_reference(args, cfg, cons)
+        return
+
+    import torch
+    dist, rank, ws = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    from apophis_gb300 import _build, hydro
+    from apophis_gb300.stepper import Stepper
+    _build.build()
+
+    zones = cfg.zones()
+    st = Stepper(cfg, cons, exact=False)
+    tune = None
+    if not args.no_tune:
+        tune = st.autotune(trial_steps=1)
+    stream = torch.cuda.current_stream()
+    st.step(args.warmup)
+    st.status()
+    # per-stage kernel durations (roofline numerator time)
+    stage_ms = st.profile(nsteps=2)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        st.step(args.steps)
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    status = st.status()
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = zones * ws / (ms * 1e-3)
+    launches_per_step = 3  # two stage kernels + the dt-policy kernel
+
+    # e2e: host buffers through the C ABI, copies inside the timed region
+    host = torch.empty(st.cons.shape, dtype=torch.float64, pin_memory=True)
+    host.copy_(st.cons)
+    nbytes = host.numel() * 8
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st.cons.copy_(host, non_blocking=True)
+        st.step(1)
+        host.copy_(st.cons, non_blocking=True)
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_value = zones * ws / (e2e_ms * 1e-3)
+    st.close()
+    del st
+    torch.cuda.empty_cache()
+
+    # plain per-meshblock launch path, bounded sample
+    plain = None
+    if rank == 0 and not args.no_plain:
+        drv = hydro.Driver(cfg, cons, exact=False, per_block=True)
+        drv.run(nsteps=1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        drv.run(nsteps=2)
+        torch.cuda.synchronize()
+        pms = (time.perf_counter() - t0) * 1e3 / 2
+        plain = {"value": zones / (pms * 1e-3), "ms_per_step": pms,
+                 "launches_per_step": 2 * cfg.nblocks * (1 + 3 + 1) + 2 + 2 + cfg.nblocks}
+        del drv
+        torch.cuda.empty_cache()
+
+    hbm, peak_kind, pk = peaks()
+    stage_sum = sum(stage_ms)
+    per_launch_bytes = BYTES_PER_ZONE_UPDATE * zones / len(stage_ms)
+    achieved = per_launch_bytes / (stage_sum / len(stage_ms) * 1e-3) / 1e9
+    clocks = clk.summary()
+    sm_mhz = clocks.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+    fp64_peak = FP64_LANES_PER_CLK_PER_SM * 152 * sm_mhz * 1e6 / 1e9  # G lane-ops/s
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "zones": zones, "meshblocks": cfg.nblocks,
+                   "parallelism": "replica per GPU" if ws > 1 else "1 GPU",
+                   "l2": "no flush: inputs larger than L2 (state 1.0 GB, ~4 GB working set)",
+                   "launch": tune["config"] if tune else None},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None,
+                     "kernel": "k_stage (batched stage)", "stage_ms": stage_ms,
+                     "peak_source": peak_kind},
+        "fp64_pipe": {"note": "the FP64 pipe binds this kernel; see profiles/",
+                      "peak_lane_ops_per_s": fp64_peak * 1e9},
+        "clocks": clocks,
+        "time_check": {"sim_time": status["time"], "ncycle": status["ncycle"]},
+    }
+    if FP64_LANE_OPS_PER_ZONE_UPDATE:
+        ach = FP64_LANE_OPS_PER_ZONE_UPDATE * zones / (stage_sum * 1e-3) / 1e9
+        line["fp64_pipe"].update({"achieved": ach, "peak": fp64_peak, "unit": "G lane-ops/s",
+                                  "frac": ach / fp64_peak})
+    if plain is not None:
+        line["plain"] = plain
+        line["batched_vs_plain"] = value / ws / plain["value"]
+    if rank == 0 and not args.no_cpu:
+        zps, cores, el = cpu_baseline(cfg, cons, 1)
+        line["cpu_baseline"] = {"value": zps, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "1 full RK2 step of the 256^3 pack after 1 warm-up "
+                                          "(%.1f s)" % el}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -129,6 +129,60 @@ aph_status aph_hydro_apply_gravity(aph_pack pack, const double g[3], double beta
  * reflecting image negates the normal momentum (apophis_boundaries.cpp:210-221). */
 aph_status aph_hydro_fill_ghosts(aph_pack pack, void *stream);
 
+/* ---- batched path ----------------------------------------------------------------
+ * A stepper advances a whole pack by full RK steps (the MultiStageDriver cycle with the
+ * stage order of ApophisDriver::MakeTaskCollection, apophis_driver.cpp:27-129): each
+ * stage is one persistent launch over every meshblock (ghost fill, ConsToPrim, the
+ * x/y/z flux passes, the update, gravity and, at the last stage, the dt reduction);
+ * dt and time stay on the device; a step is captured once as a CUDA graph and replayed.
+ * The state is the caller's cons (u0); the stepper owns u1 and its scratch.  The floors
+ * of the last FillDerived of a step are applied at the start of the next stage, so cons
+ * between steps holds the update's raw values. */
+typedef struct aph_stepper_s *aph_stepper;
+
+typedef struct aph_stepper_desc {
+  aph_hydro_params params;   /* nvar must be 5 */
+  int integrator;            /* APH_INTEGRATOR_* (parthenon/time/integrator) */
+  int nblocks;
+  const aph_block *blocks;   /* cons (state, ghosts included), nx, dx; other fields unused */
+  int nb[3];                 /* uniform block grid, blocks numbered x-fastest */
+  int bc[6];                 /* physical boundaries, as in aph_pack_set_topology */
+  int use_gravity;           /* 1: constant-g source after each update */
+  double gravity[3];
+  double tlim;               /* parthenon/time/tlim; <= 0: none */
+  double fixed_dt;           /* > 0: every step uses this dt instead of the CFL policy */
+} aph_stepper_desc;
+
+/* Launch configuration, chosen by aph_stepper_autotune or set by hand. */
+typedef struct aph_stepper_config {
+  int threads;      /* CTA size (64..256, multiple of 32) */
+  int ctas_per_sm;  /* resident CTAs per SM; 0: as many as fit */
+  int lines[3];     /* lines per work item of each direction's pass; 0: automatic */
+  int order[3];     /* sweep order (1-based directions); x, y, z in exact mode */
+  int schedule;     /* 0 strided, 1 contiguous ranges, 2 dynamic work counter */
+  int use_graph;    /* 1: replay the captured step graph */
+} aph_stepper_config;
+
+/* Allocate the stepper's scratch, run the initial FillDerived + EstimateTimestep
+ * (blocking) and set dt_0. */
+aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out);
+aph_status aph_stepper_destroy(aph_stepper stepper);
+/* Enqueue nsteps full RK steps on stream (asynchronous). */
+aph_status aph_stepper_step(aph_stepper stepper, int nsteps, void *stream);
+/* Synchronise stream and report time, the dt of the next step and the cycle count;
+ * returns APH_ERR_TIMEOUT if a stage's grid barrier gave up. */
+aph_status aph_stepper_status(aph_stepper stepper, double *time, double *dt, int *ncycle,
+                              void *stream);
+aph_status aph_stepper_get_config(aph_stepper stepper, aph_stepper_config *cfg);
+aph_status aph_stepper_set_config(aph_stepper stepper, const aph_stepper_config *cfg);
+/* Advance nsteps steps without the graph, timing each stage launch with CUDA events on
+ * stream; stage_ms[i] receives the mean duration of stage i (blocking). */
+aph_status aph_stepper_profile(aph_stepper stepper, int nsteps, double *stage_ms, void *stream);
+/* Time a built-in candidate set of configurations for trial_steps steps each on a copy
+ * of the state (the state and clock are restored) and keep the fastest. */
+aph_status aph_stepper_autotune(aph_stepper stepper, int trial_steps, aph_stepper_config *best,
+                                double *best_ms);
+
 #ifdef __cplusplus
 }
 #endif

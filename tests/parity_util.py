@@ -2,9 +2,17 @@
 
 Tolerance for the fast arithmetic mode, per cell and per variable n:
     |gpu - oracle| <= RTOL * max(|oracle|, scale_n),   RTOL = 1e-12,
-where scale_n is the largest |value| of variable n over the compared region (this keeps
-the test meaningful for quiescent components such as v_z ~ 1e-17).  The exact mode
-must match bit for bit.
+where scale_n is the largest |value| of variable n over the compared region, and for the
+three momentum components the largest |value| of any momentum component (momentum is
+one vector: a component that is born from cancellation, such as the z momentum of a
+flow that starts planar, carries the rounding of the O(|m|) terms it came from).  The
+exact mode must match bit for bit.
+
+The fast mode is held to this tolerance for one step.  Over several steps it can leave
+it: the reference's PPM limiter switches branches discontinuously (for instance between
+its extremum and overshoot formulas when a face value equals the cell average), so a
+one-ulp difference in a degenerate stencil can change a face value by the size of the
+local jump.  Multi-step bit stability is what the exact mode is for.
 """
 import numpy as np
 
@@ -26,10 +34,13 @@ def assert_parity(gpu, ref, exact, rtol=RTOL, what=""):
         return
     # per-variable scale along axis 1 (nvar) of (nblocks, nvar, ...) arrays
     nv = ref.shape[1]
+    mom = np.max(np.abs(ref[:, 1:4])) if ref.size and nv >= 4 else 0.0
     for n in range(nv):
         r = ref[:, n]
         g = gpu[:, n]
         scale = np.max(np.abs(r)) if r.size else 0.0
+        if 1 <= n <= 3:
+            scale = max(scale, mom)
         tol = rtol * np.maximum(np.abs(r), scale)
         bad = np.abs(g - r) > tol
         if bad.any():
@@ -69,3 +80,8 @@ def interior_faces(cfg, d):
     s = sl[ax]
     sl[ax] = slice(s.start, s.stop + 1)
     return tuple(sl)
+
+
+def l1_rel(gpu, ref, n=0):
+    """Mean |gpu - ref| of variable n over the mean |ref|."""
+    return float(np.mean(np.abs(gpu[:, n] - ref[:, n])) / np.mean(np.abs(ref[:, n])))

@@ -1,0 +1,131 @@
+"""The batched stepper (one persistent launch per stage, graph-replayed steps) against
+the oracle, plus its launch configuration, autotuner and error handling (needs a GPU)."""
+import numpy as np
+import pytest
+
+from apophis_gb300 import problems
+from apophis_gb300.stepper import Stepper
+from oracle import oracle as O
+from parity_util import assert_parity, l1_rel, small_workloads
+
+pytestmark = pytest.mark.gpu
+
+WORKLOADS = small_workloads()
+IDS = [w[0] for w in WORKLOADS]
+
+
+def _interior(cfg, a):
+    sk, sj, si = cfg.interior
+    return a[:, :, sk, sj, si]
+
+
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+@pytest.mark.parametrize("wl", WORKLOADS, ids=IDS)
+def test_stepper_matches_oracle(cuda, wl, exact):
+    name, cfg, cons = wl
+    m = O.Mesh(cfg)
+    m.set_cons(cons)
+    st = Stepper(cfg, cons, exact=exact)
+    s0 = st.status()
+    if exact:
+        assert s0["dt"] == m.state()["dt"]
+    for step in range(3):
+        m.run(nsteps=1)
+        st.step(1)
+        s = st.status()
+        ref = m.state()
+        assert s["ncycle"] == ref["ncycle"]
+        if exact:
+            assert s["dt"] == ref["dt"] and s["time"] == ref["time"]
+            assert_parity(_interior(cfg, st.state()), _interior(cfg, m.get("cons")), True,
+                          what="cons step %d" % step)
+        else:
+            assert abs(s["dt"] - ref["dt"]) <= 1e-12 * ref["dt"]
+            if step == 0:
+                assert_parity(_interior(cfg, st.state()), _interior(cfg, m.get("cons")), False)
+            else:
+                assert l1_rel(_interior(cfg, st.state()), _interior(cfg, m.get("cons"))) < 1e-6
+    st.close()
+
+
+@pytest.mark.parametrize("integ", ["rk1", "rk3", "vl2"])
+def test_stepper_integrators_exact(cuda, integ):
+    cfg, cons = problems.kh2d(n=32, block=16, ng=3, recon="ppm", rsolver="hllc",
+                              integrator=integ)
+    m = O.Mesh(cfg)
+    m.set_cons(cons)
+    st = Stepper(cfg, cons, exact=True)
+    m.run(nsteps=3)
+    st.step(3)
+    assert st.status()["dt"] == m.state()["dt"]
+    assert_parity(_interior(cfg, st.state()), _interior(cfg, m.get("cons")), True)
+
+
+def test_stepper_sod_to_tlim(cuda):
+    """configs[0]: Sod 1D to t = 0.2 in the batched path, L1(rho) vs oracle < 1e-10."""
+    cfg, cons = problems.sod(nx=256, recon="plm", rsolver="hlle", integrator="rk2", cfl=0.4)
+    m = O.Mesh(cfg)
+    m.set_cons(cons)
+    m.run(tlim=0.2)
+    st = Stepper(cfg, cons, exact=False, tlim=0.2)
+    s = st.run(tlim=0.2)
+    assert s["ncycle"] == m.state()["ncycle"]
+    assert abs(s["time"] - 0.2) < 1e-14
+    g = cfg.ng
+    l1 = np.mean(np.abs(st.state()[0, 0, 0, 0, g:-g] - m.get("cons")[0, 0, 0, 0, g:-g]))
+    assert l1 < 1e-10
+
+
+def test_stepper_configs_agree(cuda):
+    """Every schedule / CTA size / lines-per-item choice gives the same bits (exact)."""
+    cfg, cons = problems.kh3d(n=16, block=8, ng=4)
+    ref = None
+    for cfgd in [dict(threads=256, schedule=0, lines=[0, 0, 0]),
+                 dict(threads=128, schedule=1, lines=[3, 5, 2]),
+                 dict(threads=256, schedule=2, lines=[1, 1, 1])]:
+        st = Stepper(cfg, cons, exact=True)
+        c = st.config
+        c.update(cfgd)
+        st.set_config(c)
+        st.step(2)
+        out = _interior(cfg, st.state())
+        if ref is None:
+            ref = out
+        else:
+            assert np.array_equal(out, ref)
+        st.close()
+
+
+def test_stepper_sweep_order_fast(cuda):
+    cfg, cons = problems.kh3d(n=16, block=8, ng=4)
+    m = O.Mesh(cfg)
+    m.set_cons(cons)
+    m.run(nsteps=1)
+    st = Stepper(cfg, cons, exact=False)
+    c = st.config
+    c["order"] = [3, 1, 2]
+    st.set_config(c)
+    st.step(1)
+    assert_parity(_interior(cfg, st.state()), _interior(cfg, m.get("cons")), False)
+    st2 = Stepper(cfg, cons, exact=True)
+    c = st2.config
+    c["order"] = [2, 1, 3]
+    with pytest.raises(Exception):
+        st2.set_config(c)
+
+
+def test_stepper_autotune_keeps_state(cuda, tmp_path):
+    cfg, cons = problems.kh2d(n=64, block=32, ng=3, recon="ppm", rsolver="hllc")
+    m = O.Mesh(cfg)
+    m.set_cons(cons)
+    m.run(nsteps=2)
+    st = Stepper(cfg, cons, exact=True)
+    rec = st.autotune(trial_steps=1, cache=str(tmp_path / "tune.json"))
+    assert rec["ms_per_step"] > 0
+    assert st.status()["ncycle"] == 0
+    st.step(2)
+    assert_parity(_interior(cfg, st.state()), _interior(cfg, m.get("cons")), True)
+    # the cached record is reused
+    st2 = Stepper(cfg, cons, exact=True)
+    rec2 = st2.autotune(trial_steps=1, cache=str(tmp_path / "tune.json"))
+    assert rec2["config"] == rec["config"]
