@@ -31,6 +31,7 @@ UNITS = {
     "aph_stage_fast.cu": [],
     "aph_stage_exact.cu": ["--fmad=false"],
     "aph_stepper.cu": [],
+    "aph_adjoint.cu": [],
 }
 
 

@@ -102,6 +102,17 @@ SIGNATURES = {
     "aph_stepper_profile": ([ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_autotune": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(aph_stepper_config),
                               _dp], ctypes.c_int),
+    "aph_adjoint_create": ([ctypes.POINTER(aph_stepper_desc), ctypes.POINTER(ctypes.c_void_p)],
+                           ctypes.c_int),
+    "aph_adjoint_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "aph_adjoint_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
+                          ctypes.c_void_p], ctypes.c_int),
+    "aph_adjoint_step_vjp": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "aph_adjoint_forward": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int,
+                             ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "aph_adjoint_backward": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+                             ctypes.c_int),
 }
 EXTRA_SIGNATURES = {}
 

@@ -74,7 +74,11 @@ __device__ __noinline__ bool grid_barrier(StepCtl *ctl, unsigned long long timeo
 struct Sched {
   int mode;
   __device__ __forceinline__ int first(unsigned int *ctr, int n) const {
-    if (mode == 1) return (int)(((long long)blockIdx.x * n) / gridDim.x);
+    if (mode == 1) {  // this CTA's contiguous range, possibly empty
+      const int s = (int)(((long long)blockIdx.x * n) / gridDim.x);
+      const int e = (int)(((long long)(blockIdx.x + 1) * n) / gridDim.x);
+      return s < e ? s : n;
+    }
     if (mode == 2) return next(ctr, n, -1);
     return blockIdx.x;
   }

@@ -41,11 +41,13 @@ UNIT = "zone-updates/s"
 WORKLOAD = ("kh3d 256^3: 64 meshblocks of 64^3, 4 ghost cells, PPM+HLLC, RK2, CFL 0.3, "
             "gamma 5/3, FP64")
 BYTES_PER_ZONE_UPDATE = 200.0   # RK2 with 5 FP64 conserved variables
-# FP64 instructions per zone-update of the stage kernel (fast mode), from the ncu
-# capture summarised in profiles/stage_kernel_kh3d.md (sm__inst_executed_pipe_fp64 per
-# zone-update; one warp instruction = 32 lane operations)
-FP64_LANE_OPS_PER_ZONE_UPDATE = None
-FP64_LANES_PER_CLK_PER_SM = 2.05   # measured DFMA rate on GB300 (profiles/fp64_pipe_gb300.md)
+# FP64 work of the stage kernel (fast mode) per RK2 zone-update: DADD + DMUL + DFMA thread
+# instructions from the ncu capture in profiles/stage_kernel_kh3d.md (1,298 per zone per stage)
+FP64_LANE_OPS_PER_ZONE_UPDATE = 2597.0
+FP64_LANES_PER_CLK_PER_SM = 2.0    # DFMA lanes per clock per SM on GB300 (profiles/fp64_pipe_gb300.md)
+# DRAM bytes (read + write) per zone per stage launch, same capture (128^3 pack of 64^3 blocks;
+# the 256^3 launches process the same blocks, 8x as many)
+TRAFFIC_BYTES_PER_ZONE_LAUNCH = 613.8
 
 
 def peaks():
@@ -261,11 +263,13 @@ def main():
                 "d2h_bytes_per_step": nbytes},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None,
+                     "frac": achieved / hbm,
+                     "traffic": TRAFFIC_BYTES_PER_ZONE_LAUNCH * zones,
+                     "traffic_note": "ncu DRAM bytes per zone of a 128^3 capture x zones",
                      "kernel": "k_stage (batched stage)", "stage_ms": stage_ms,
                      "peak_source": peak_kind},
-        "fp64_pipe": {"note": "the FP64 pipe binds this kernel; see profiles/",
-                      "peak_lane_ops_per_s": fp64_peak * 1e9},
+        "fp64_pipe": {"note": "the FP64 pipe binds this kernel (ncu: 82 % busy, DRAM 2 %)",
+                      "peak_source": "2 DFMA lanes/clk/SM x 152 SMs x sampled SM clock"},
         "clocks": clocks,
         "time_check": {"sim_time": status["time"], "ncycle": status["ncycle"]},
     }

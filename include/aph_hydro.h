@@ -183,6 +183,34 @@ aph_status aph_stepper_profile(aph_stepper stepper, int nsteps, double *stage_ms
 aph_status aph_stepper_autotune(aph_stepper stepper, int trial_steps, aph_stepper_config *best,
                                 double *best_ms);
 
+/* ---- adjoint of the step --------------------------------------------------------------
+ * Hand-written reverse mode of the full fixed-dt step: ConsToPrim, the PLM (or donor-cell)
+ * limiter, the HLLE / HLLC fluxes with their wave-speed and contact branches, the flux
+ * divergence, the RK stage combination and the ghost map.  No counterpart in the
+ * reference (which has no derivatives); it differentiates the path the entry points above
+ * implement.  All state arguments are device arrays in pack layout: nblocks consecutive
+ * meshblocks of (5, nk, nj, ni) doubles, ghost entries ignored on input and zero in
+ * adjoint outputs.  The pack is described by an aph_stepper_desc (its cons pointers are
+ * not used: the adjoint owns its buffers); dc or plm, hlle or hllc, no gravity, nvar 5. */
+typedef struct aph_adjoint_s *aph_adjoint;
+aph_status aph_adjoint_create(const aph_stepper_desc *desc, aph_adjoint *out);
+aph_status aph_adjoint_destroy(aph_adjoint adjoint);
+/* One RK step with fixed dt: u_next = step(u_n) (the forward the adjoint linearises). */
+aph_status aph_adjoint_step(aph_adjoint adjoint, const double *u_n, double dt, double *u_next,
+                            void *stream);
+/* Vector-Jacobian product of one step: lam_n = (dU^{n+1}/dU^n)^T lam_next (lam_n may alias
+ * lam_next).  Returns APH_ERR_STATE if a floor fired in the step. */
+aph_status aph_adjoint_step_vjp(aph_adjoint adjoint, const double *u_n, double dt,
+                                const double *lam_next, double *lam_n, void *stream);
+/* Rollout of nsteps steps with the fixed dt schedule dts[] (host array) from u0, keeping a
+ * checkpoint every checkpoint_every steps on the device; writes the final state. */
+aph_status aph_adjoint_forward(aph_adjoint adjoint, const double *u0, int nsteps, const double *dts,
+                               int checkpoint_every, double *u_final, void *stream);
+/* Reverse sweep of the last rollout: recompute each segment from its checkpoint, then the
+ * step VJPs backwards; lam_initial = (dU^N/dU^0)^T lam_final (blocking). */
+aph_status aph_adjoint_backward(aph_adjoint adjoint, const double *lam_final, double *lam_initial,
+                                void *stream);
+
 #ifdef __cplusplus
 }
 #endif
