@@ -32,6 +32,7 @@ UNITS = {
     "aph_stage_exact.cu": ["--fmad=false"],
     "aph_stepper.cu": [],
     "aph_adjoint.cu": [],
+    "aph_noalloc.cu": [],
 }
 
 

@@ -89,6 +89,10 @@ SIGNATURES = {
     "aph_hydro_apply_gravity": ([ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_void_p],
                                 ctypes.c_int),
     "aph_hydro_fill_ghosts": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "aph_hydro_estimate_timestep_noalloc": ([ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                             ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_create": ([ctypes.POINTER(aph_stepper_desc), ctypes.POINTER(ctypes.c_void_p)],
                            ctypes.c_int),
     "aph_stepper_destroy": ([ctypes.c_void_p], ctypes.c_int),
