@@ -30,12 +30,19 @@ class aph_hydro_params(ctypes.Structure):
                 ("cfl", ctypes.c_double), ("exact", ctypes.c_int)]
 
 
+class aph_amr_block(ctypes.Structure):
+    _fields_ = [("level", ctypes.c_int), ("origin", ctypes.c_int * 2),
+                ("face_kind", ctypes.c_int * 4), ("face_count", ctypes.c_int * 4),
+                ("face_nbr", (ctypes.c_int * 4) * 4)]
+
+
 class aph_stepper_desc(ctypes.Structure):
     _fields_ = [("params", aph_hydro_params), ("integrator", ctypes.c_int),
                 ("nblocks", ctypes.c_int), ("blocks", ctypes.POINTER(aph_block)),
                 ("nb", ctypes.c_int * 3), ("bc", ctypes.c_int * 6),
                 ("use_gravity", ctypes.c_int), ("gravity", ctypes.c_double * 3),
-                ("tlim", ctypes.c_double), ("fixed_dt", ctypes.c_double)]
+                ("tlim", ctypes.c_double), ("fixed_dt", ctypes.c_double),
+                ("amr", ctypes.POINTER(aph_amr_block))]
 
 
 class aph_stepper_config(ctypes.Structure):
@@ -74,6 +81,12 @@ SIGNATURES = {
                          ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "aph_pack_set_topology": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
                                ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "aph_pack_set_amr": ([ctypes.c_void_p, ctypes.POINTER(aph_amr_block),
+                          ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "aph_amr_check": ([ctypes.POINTER(aph_amr_block), ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                       ctypes.c_int], ctypes.c_int),
+    "aph_pack_partition": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                            ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "aph_pack_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "aph_hydro_cons_to_prim": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "aph_hydro_calculate_fluxes": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],

@@ -77,9 +77,69 @@ struct aph_pack_s {
   int max_ncell = 0, max_interior = 0;
   bool uniform = true;
   bool has_topology = false;
+  aph_pack parent = nullptr;  // a partition shares its parent's descriptors
+  int children = 0;           // live partitions of this pack
 };
 
 namespace aph {
+const char *amr_check(int nb, const AmrFaces *F, const int (*nx)[2], int ng, char *msg, size_t len) {
+  for (int b = 0; b < nb; ++b) {
+    const AmrFaces &A = F[b];
+    if (nx[b][0] < 2 * ng || nx[b][1] < 2 * ng) {
+      snprintf(msg, len, "block %d: refined meshes need >= 2*nghost cells per side", b);
+      return msg;
+    }
+    for (int f = 0; f < 4; ++f) {
+      const int d = f / 2, td = 1 - d, kind = A.kind[f];
+      if (kind < FACE_SAME || kind > FACE_BOUNDARY) {
+        snprintf(msg, len, "block %d face %d: kind %d", b, f, kind);
+        return msg;
+      }
+      const int need = kind == FACE_BOUNDARY ? 0 : 1;
+      const int maxn = kind == FACE_FINER ? 4 : need;
+      if (A.cnt[f] < need || A.cnt[f] > maxn) {
+        snprintf(msg, len, "block %d face %d: %d neighbours", b, f, A.cnt[f]);
+        return msg;
+      }
+      for (int n = 0; n < A.cnt[f]; ++n)
+        if (A.nbr[f][n] < 0 || A.nbr[f][n] >= nb) {
+          snprintf(msg, len, "block %d face %d: neighbour out of range", b, f);
+          return msg;
+        }
+      const int t0 = A.origin[td], t1 = A.origin[td] + nx[b][td];
+      if (kind == FACE_SAME) {
+        const int m = A.nbr[f][0];
+        if (F[m].level != A.level || F[m].origin[td] > t0 || F[m].origin[td] + nx[m][td] < t1) {
+          snprintf(msg, len, "block %d face %d: same-level neighbour does not cover the face", b, f);
+          return msg;
+        }
+      } else if (kind == FACE_COARSER) {
+        const int m = A.nbr[f][0];
+        if (F[m].level != A.level - 1 || (t0 & 1) || (nx[b][td] & 1) ||
+            F[m].origin[td] > (t0 >> 1) || F[m].origin[td] + nx[m][td] < (t1 >> 1)) {
+          snprintf(msg, len, "block %d face %d: coarser neighbour does not cover the face", b, f);
+          return msg;
+        }
+      } else if (kind == FACE_FINER) {
+        // every fine cell pair (2t, 2t+1) lies in one listed neighbour
+        for (int t = t0; t < t1; ++t) {
+          bool ok = false;
+          for (int n = 0; n < A.cnt[f]; ++n) {
+            const int m = A.nbr[f][n];
+            ok |= F[m].level == A.level + 1 && F[m].origin[td] <= 2 * t &&
+                  2 * t + 1 < F[m].origin[td] + nx[m][td];
+          }
+          if (!ok) {
+            snprintf(msg, len, "block %d face %d: finer neighbours do not cover the face", b, f);
+            return msg;
+          }
+        }
+      }
+    }
+  }
+  return nullptr;
+}
+
 const BlockDev *pack_blocks(aph_pack p) { return p->d_blocks; }
 const PackDev &pack_dev(aph_pack p) { return p->dev; }
 int pack_max_interior(aph_pack p) { return p->max_interior; }
@@ -199,8 +259,94 @@ aph_status aph_pack_set_topology(aph_pack p, const int nb[3], const int bc[6]) {
   return APH_OK;
 }
 
+aph_status aph_pack_set_amr(aph_pack p, const aph_amr_block *amr, const int bc[6]) {
+  clear_error();
+  if (!p || !amr || !bc) return fail(APH_ERR_INVALID, "NULL argument");
+  if (p->parent) return fail(APH_ERR_INVALID, "set the mesh on the parent pack");
+  if (p->dev.ndim != 2 || p->dev.nvar != 5)
+    return fail(APH_ERR_UNSUPPORTED, "refined meshes are 2D with 5 variables");
+  if (p->children) return fail(APH_ERR_INVALID, "set the mesh before partitioning the pack");
+  const int nb = p->dev.nblocks;
+  static_assert(sizeof(AmrFaces) == sizeof(aph_amr_block), "face table layout");
+  std::vector<AmrFaces> faces(nb);
+  std::vector<int> nxs(2 * nb);
+  for (int b = 0; b < nb; ++b) {
+    std::memcpy(&faces[b], &amr[b], sizeof(AmrFaces));
+    nxs[2 * b] = p->host_blocks[b].nx[0];
+    nxs[2 * b + 1] = p->host_blocks[b].nx[1];
+  }
+  char msg[160];
+  if (amr_check(nb, faces.data(), (const int(*)[2])nxs.data(), p->dev.ng, msg, sizeof(msg)))
+    return fail(APH_ERR_INVALID, "%s", msg);
+  for (int d = 0; d < 2; ++d)
+    for (int s = 0; s < 2; ++s)
+      if (bc[2 * d + s] < 0 || bc[2 * d + s] > 2)
+        return fail(APH_ERR_INVALID, "boundary condition %d not recognized", bc[2 * d + s]);
+  for (int b = 0; b < nb; ++b) p->host_blocks[b].amr = faces[b];
+  for (int d = 0; d < 3; ++d) {
+    p->dev.bc[d][0] = bc[2 * d];
+    p->dev.bc[d][1] = bc[2 * d + 1];
+  }
+  p->dev.amr = 1;
+  cudaError_t e = cudaMemcpy(p->d_blocks, p->host_blocks.data(), sizeof(BlockDev) * nb,
+                             cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "aph_pack_set_amr");
+  p->has_topology = true;
+  return APH_OK;
+}
+
+aph_status aph_amr_check(const aph_amr_block *amr, const int *nx, int nblocks, int nghost) {
+  clear_error();
+  if (!amr || !nx || nblocks <= 0 || nghost < 1) return fail(APH_ERR_INVALID, "bad argument");
+  std::vector<AmrFaces> faces(nblocks);
+  for (int b = 0; b < nblocks; ++b) std::memcpy(&faces[b], &amr[b], sizeof(AmrFaces));
+  char msg[160];
+  if (amr_check(nblocks, faces.data(), (const int(*)[2])nx, nghost, msg, sizeof(msg)))
+    return fail(APH_ERR_INVALID, "%s", msg);
+  return APH_OK;
+}
+
+aph_status aph_pack_partition(aph_pack parent, int first, int count, aph_pack *out) {
+  clear_error();
+  if (!parent || !out) return fail(APH_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (parent->parent) return fail(APH_ERR_INVALID, "partition of a partition");
+  if (first < 0 || count < 1 || first + count > parent->dev.nblocks)
+    return fail(APH_ERR_INVALID, "blocks %d..%d outside the pack", first, first + count - 1);
+  aph_pack p = new aph_pack_s();
+  p->params = parent->params;
+  p->dev = parent->dev;
+  p->dev.block0 = first;
+  p->dev.nblocks = count;
+  p->host_blocks.assign(parent->host_blocks.begin() + first, parent->host_blocks.begin() + first + count);
+  p->d_blocks = parent->d_blocks;
+  p->parent = parent;
+  parent->children++;
+  p->uniform = parent->uniform;
+  p->has_topology = parent->has_topology;
+  for (const BlockDev &B : p->host_blocks) {
+    p->max_ncell = std::max<long long>(p->max_ncell, B.ncell);
+    p->max_interior = std::max(p->max_interior, B.nx[0] * B.nx[1] * B.nx[2]);
+  }
+  cudaError_t e = cudaMalloc(&p->d_scratch, 4 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_dt, 2 * sizeof(double));
+  if (e != cudaSuccess) {
+    aph_pack_destroy(p);
+    return cuda_fail(e, "aph_pack_partition");
+  }
+  *out = p;
+  return APH_OK;
+}
+
 aph_status aph_pack_destroy(aph_pack p) {
+  clear_error();
   if (!p) return APH_OK;
+  if (p->children)
+    return fail(APH_ERR_INVALID, "pack has %d live partitions: destroy them first", p->children);
+  if (p->parent) {
+    p->parent->children--;
+    p->d_blocks = nullptr;
+  }
   if (p->d_blocks) cudaFree(p->d_blocks);
   if (p->d_scratch) cudaFree(p->d_scratch);
   if (p->d_dt) cudaFree(p->d_dt);

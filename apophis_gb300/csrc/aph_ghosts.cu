@@ -1,5 +1,6 @@
 // aph_ghosts.cu -- ghost-zone fill on a uniform block grid: same-level exchange and the
 // periodic / outflow / reflecting physical boundaries in one pass.  Integer work only.
+#include "aph_amr.cuh"
 #include "aph_capi_internal.h"
 
 namespace aph {
@@ -22,7 +23,7 @@ __device__ __forceinline__ int map_index(int g, int n, int lo, int hi, bool &fli
 }
 
 __global__ void __launch_bounds__(256) k_fill_ghosts(PackDev p, const BlockDev *blocks, int field) {
-  const BlockDev &B = blocks[blockIdx.y];
+  const BlockDev &B = blocks[p.block0 + blockIdx.y];
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= B.ncell) return;
   const int idx[3] = {(int)(c % B.ni), (int)((c / B.ni) % B.nj), (int)(c / ((long long)B.ni * B.nj))};
@@ -54,10 +55,20 @@ __global__ void __launch_bounds__(256) k_fill_ghosts(PackDev p, const BlockDev *
   }
 }
 
+__global__ void __launch_bounds__(256) k_fill_ghosts_amr(PackDev p, const BlockDev *blocks) {
+  const BlockDev &B = blocks[p.block0 + blockIdx.y];
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= B.ncell) return;
+  amr_fill_cell(blocks, B, [](const BlockDev &X) -> const double * { return X.cons; }, p.bc, p.ng, c);
+}
+
 cudaError_t launch_fill_ghosts(const PackDev &p, const BlockDev *blocks, int max_ncell, int field,
                                cudaStream_t s) {
   dim3 grid((unsigned)((max_ncell + 255) / 256), p.nblocks);
-  k_fill_ghosts<<<grid, 256, 0, s>>>(p, blocks, field);
+  if (p.amr)
+    k_fill_ghosts_amr<<<grid, 256, 0, s>>>(p, blocks);
+  else
+    k_fill_ghosts<<<grid, 256, 0, s>>>(p, blocks, field);
   return cudaGetLastError();
 }
 

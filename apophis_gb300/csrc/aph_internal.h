@@ -7,6 +7,22 @@
 
 namespace aph {
 
+// Neighbours of a meshblock on a statically refined 2D mesh (face order x-, x+, y-, y+).
+constexpr int FACE_SAME = 0, FACE_COARSER = 1, FACE_FINER = 2, FACE_BOUNDARY = 3;
+struct AmrFaces {
+  int level;
+  int origin[2];      // global index of the first interior cell, in cells of its level
+  int kind[4];
+  int cnt[4];
+  int nbr[4][4];
+};
+
+// Host-side check of a refined mesh's face table against the blocks' sizes, before any
+// kernel reads through it: every index the ghost fill and the flux correction form must land
+// in the named block's interior.  Returns nullptr, or a message (written to msg).
+const char *amr_check(int nblocks, const AmrFaces *faces, const int (*nx)[2], int ng, char *msg,
+                      size_t len);
+
 // Device copy of one meshblock's descriptor.
 struct BlockDev {
   double *cons, *prim, *gamma, *u1;
@@ -16,6 +32,7 @@ struct BlockDev {
   int loc[3];         // logical block position in the block grid
   double dx[3];
   long long ncell;    // ni * nj * nk
+  AmrFaces amr;
 };
 
 // Per-pack constants.
@@ -28,6 +45,8 @@ struct PackDev {
   int nb[3];          // blocks per dimension (uniform grids; 0 when unknown)
   int bc[3][2];       // physical boundary per face
   int mesh_nx[3];
+  int amr;            // 1: blocks carry AmrFaces (statically refined 2D mesh)
+  int block0;         // first block of this launch (a partition of the pack)
 };
 
 // ---- batched stepper -----------------------------------------------------------
@@ -36,11 +55,13 @@ struct PackDev {
 // (entire domain) and the accumulated flux difference du (interior only).
 struct StepBlock {
   double *u0, *u1, *prim, *gamma, *du;
+  double *bflux;      // refined meshes: fluxes of the 4 boundary faces, [face][t][5]
   int nx[3];
   int ni, nj, nk;
   int loc[3];
   long long ncell, nint;
   double dx[3];
+  AmrFaces amr;
 };
 
 // Device-resident control block of a stepper (dt and time live on the device so that a
@@ -67,6 +88,9 @@ struct StageArgs {
   int ncell_items;
   const int2 *line_items[3];    // per direction: (block, first line) of T[d] lines
   int nline_items[3];
+  const int *fix_items;         // refined meshes: blocks with a finer neighbour
+  int nfix_items;
+  int bflux_stride;             // doubles per face of bflux (max transverse cells * 5)
   int T[3];
   int order[3];                 // sweep order (1-based directions)
   double gam0, gam1, beta;

@@ -4,6 +4,7 @@
 // Included once per arithmetic mode with APH_NS naming the namespace
 // (aph_fast.cu, aph_exact.cu).
 #pragma once
+#include "aph_amr.cuh"
 #include "aph_internal.h"
 #include "aph_math.cuh"
 
@@ -24,7 +25,7 @@ __device__ __forceinline__ int dim_start(int d, int ndim, int ng) { return d < n
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_cons_to_prim(PackDev p, const BlockDev *blocks,
                                                            int *floor_flag) {
-  const BlockDev &B = blocks[blockIdx.y];
+  const BlockDev &B = blocks[p.block0 + blockIdx.y];
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= B.ncell) return;
   const long long nc = B.ncell;
@@ -94,7 +95,7 @@ __device__ __forceinline__ void line_geometry(const BlockDev &B, int ndim, int n
 template <int DIR, int RECON, int RS>
 __global__ void __launch_bounds__(kThreads) k_fluxes(PackDev p, const BlockDev *blocks, int T) {
   extern __shared__ double sm[];
-  const BlockDev &B = blocks[blockIdx.y];
+  const BlockDev &B = blocks[p.block0 + blockIdx.y];
   const int ntrans = (DIR == 1) ? B.nx[1] * B.nx[2] : (DIR == 2) ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1];
   const int line0 = blockIdx.x * T;
   if (line0 >= ntrans) return;
@@ -187,7 +188,7 @@ __device__ __forceinline__ bool interior_cell(const BlockDev &B, int ndim, int n
 __global__ void __launch_bounds__(kThreads) k_update(PackDev p, const BlockDev *blocks,
                                                      double gam0, double gam1, double beta,
                                                      double beta_dt_host, const double *dt_dev) {
-  const BlockDev &B = blocks[blockIdx.y];
+  const BlockDev &B = blocks[p.block0 + blockIdx.y];
   long long c;
   if (!interior_cell(B, p.ndim, p.ng, blockIdx.x * blockDim.x + threadIdx.x, c)) return;
   const double beta_dt = dt_dev ? beta * dt_dev[0] : beta_dt_host;
@@ -200,6 +201,46 @@ __global__ void __launch_bounds__(kThreads) k_update(PackDev p, const BlockDev *
     double du = (a1 * B.flux[0][q + 1] - a1 * B.flux[0][q]);
     if (p.ndim >= 2) du += (a2 * B.flux[1][q + sj] - a2 * B.flux[1][q]);
     if (p.ndim == 3) du += (a3 * B.flux[2][q + sk] - a3 * B.flux[2][q]);
+    const double div = -du / vol;
+    B.cons[q] = gam0 * B.cons[q] + gam1 * B.u1[q] + beta_dt * div;
+  }
+}
+
+// Refined 2D meshes: the same update with the coarse-fine correction of each coarse
+// boundary cell's flux difference to the mean of the fine face fluxes (faces x-, x+, y-, y+).
+__global__ void __launch_bounds__(kThreads) k_update_amr(PackDev p, const BlockDev *blocks,
+                                                         double gam0, double gam1, double beta,
+                                                         double beta_dt_host, const double *dt_dev) {
+  const BlockDev &B = blocks[p.block0 + blockIdx.y];
+  long long c;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!interior_cell(B, p.ndim, p.ng, idx, c)) return;
+  const int ii = idx % B.nx[0], jj = idx / B.nx[0];
+  const double beta_dt = dt_dev ? beta * dt_dev[0] : beta_dt_host;
+  const double a1 = B.dx[1] * B.dx[2], a2 = B.dx[0] * B.dx[2];
+  const double vol = B.dx[0] * B.dx[1] * B.dx[2];
+  const long long nc = B.ncell;
+  for (int n = 0; n < p.nvar; ++n) {
+    const long long q = n * nc + c;
+    double du = (a1 * B.flux[0][q + 1] - a1 * B.flux[0][q]);
+    du += (a2 * B.flux[1][q + B.ni] - a2 * B.flux[1][q]);
+    for (int face = 0; face < 4; ++face) {
+      if (B.amr.kind[face] != FACE_FINER) continue;
+      const int d = face / 2, s = face % 2, td = 1 - d;
+      const int a = d == 0 ? ii : jj, t = d == 0 ? jj : ii;
+      if (a != (s == 0 ? 0 : B.nx[d] - 1)) continue;
+      const double area = d == 0 ? a1 : a2;
+      const int tg2 = 2 * (B.amr.origin[td] + t);
+      const BlockDev &F = amr_fine_nbr(blocks, B, face, td, tg2);
+      const int ft = tg2 - F.amr.origin[td];
+      const long long fo = n * B.ncell + amr_cell(B, p.ng, d, s == 0 ? 0 : B.nx[d], t);
+      const int ffa = s == 0 ? F.nx[d] : 0;
+      const long long f0 = n * F.ncell + amr_cell(F, p.ng, d, ffa, ft);
+      const long long f1 = n * F.ncell + amr_cell(F, p.ng, d, ffa, ft + 1);
+      const double Fold = B.flux[d][fo];
+      const double Fnew = 0.5 * (F.flux[d][f0] + F.flux[d][f1]);
+      du = s == 0 ? du + (area * Fold - area * Fnew) : du + (area * Fnew - area * Fold);
+    }
     const double div = -du / vol;
     B.cons[q] = gam0 * B.cons[q] + gam1 * B.u1[q] + beta_dt * div;
   }
@@ -232,7 +273,7 @@ __device__ __forceinline__ unsigned long long block_min_bits(unsigned long long 
 
 __global__ void __launch_bounds__(kThreads) k_estimate_dt(PackDev p, const BlockDev *blocks,
                                                           unsigned long long *min_bits) {
-  const BlockDev &B = blocks[blockIdx.y];
+  const BlockDev &B = blocks[p.block0 + blockIdx.y];
   long long c;
   unsigned long long v = ~0ULL;
   if (interior_cell(B, p.ndim, p.ng, blockIdx.x * blockDim.x + threadIdx.x, c)) {
@@ -256,7 +297,7 @@ __global__ void __launch_bounds__(kThreads) k_apply_gravity(PackDev p, const Blo
                                                             double g0, double g1, double g2,
                                                             double beta, double beta_dt_host,
                                                             const double *dt_dev) {
-  const BlockDev &B = blocks[blockIdx.y];
+  const BlockDev &B = blocks[p.block0 + blockIdx.y];
   long long c;
   if (!interior_cell(B, p.ndim, p.ng, blockIdx.x * blockDim.x + threadIdx.x, c)) return;
   const double dt = dt_dev ? beta * dt_dev[0] : beta_dt_host;
@@ -344,7 +385,10 @@ cudaError_t launch_update(const PackDev &p, const BlockDev *blocks, double gam0,
                           double beta, double beta_dt_host, const double *dt_dev,
                           int max_interior, cudaStream_t s) {
   dim3 grid(cdiv(max_interior, kThreads), p.nblocks);
-  k_update<<<grid, kThreads, 0, s>>>(p, blocks, gam0, gam1, beta, beta_dt_host, dt_dev);
+  if (p.amr)
+    k_update_amr<<<grid, kThreads, 0, s>>>(p, blocks, gam0, gam1, beta, beta_dt_host, dt_dev);
+  else
+    k_update<<<grid, kThreads, 0, s>>>(p, blocks, gam0, gam1, beta, beta_dt_host, dt_dev);
   return cudaGetLastError();
 }
 

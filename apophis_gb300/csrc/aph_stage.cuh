@@ -15,6 +15,7 @@
 // ghost rows, one evaluation per face value, constant adiabatic indices when no floor
 // fired, predicates on the integer pipe.
 #pragma once
+#include "aph_amr.cuh"
 #include "aph_internal.h"
 #include "aph_math.cuh"
 
@@ -349,12 +350,21 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
     }
   }
   __syncthreads();
+  if (a.p.amr) {  // keep the boundary-face fluxes of every line for the coarse-fine correction
+    const int w1 = n + 1;
+    const size_t fs = (size_t)T * w1;
+    for (int it = tid; it < nl * 2 * NHYDRO; it += nth) {
+      const int t = it / (2 * NHYDRO), r = it % (2 * NHYDRO), side = r / NHYDRO, v = r % NHYDRO;
+      B.bflux[(size_t)(2 * (DIR - 1) + side) * a.bflux_stride + (size_t)(l0 + t) * NHYDRO + v] =
+          F[v * fs + (size_t)t * w1 + (side == 0 ? 0 : n)];
+    }
+  }
   // F: flux difference of each interior cell; du accumulates x, y, z in order
   {
     const int w1 = n + 1;
     const size_t fs = (size_t)T * w1;
     const double area = DIR == 1 ? B.dx[1] * B.dx[2] : DIR == 2 ? B.dx[0] * B.dx[2] : B.dx[0] * B.dx[1];
-    if (!last_pass) {
+    if (!last_pass || a.p.amr) {
       for (int it = tid; it < NHYDRO * nl * n; it += nth) {
         const int v = it / (nl * n);
         const int r = it - v * nl * n;
@@ -412,6 +422,74 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
   __syncthreads();
 }
 
+// Refined meshes: conservation at coarse-fine faces.  Each coarse block with a finer
+// neighbour corrects its boundary cells' flux differences from its own face flux to the mean
+// of the fine face fluxes, faces in the order x-, x+, y-, y+.
+__device__ void amr_correct(const StageArgs &a, const Sched &sched, unsigned int *ctr) {
+  for (int it = sched.first(ctr, a.nfix_items); it < a.nfix_items; it = sched.next(ctr, a.nfix_items, it)) {
+    const StepBlock &B = a.blocks[a.fix_items[it]];
+    for (int face = 0; face < 4; ++face) {
+      if (B.amr.kind[face] != FACE_FINER) continue;
+      const int d = face / 2, s = face % 2, td = 1 - d;
+      const double area = d == 0 ? B.dx[1] * B.dx[2] : B.dx[0] * B.dx[2];
+      for (int it2 = threadIdx.x; it2 < B.nx[td] * NHYDRO; it2 += blockDim.x) {
+        const int t = it2 / NHYDRO, v = it2 % NHYDRO;
+        const int tg2 = 2 * (B.amr.origin[td] + t);
+        const StepBlock &F = amr_fine_nbr(a.blocks, B, face, td, tg2);
+        const int ft = tg2 - F.amr.origin[td];
+        const double *fb = F.bflux + (size_t)(2 * d + 1 - s) * a.bflux_stride;
+        const double Fold = B.bflux[(size_t)face * a.bflux_stride + (size_t)t * NHYDRO + v];
+        const double Fnew = 0.5 * (fb[(size_t)ft * NHYDRO + v] + fb[(size_t)(ft + 1) * NHYDRO + v]);
+        const int ca = s == 0 ? 0 : B.nx[d] - 1;
+        const int i = d == 0 ? ca : t, j = d == 0 ? t : ca;
+        double &x = B.du[v * B.nint + (long long)j * B.nx[0] + i];
+        x = s == 0 ? x + (area * Fold - area * Fnew) : x + (area * Fnew - area * Fold);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Refined meshes: the RK update, gravity and dt candidates after the correction.
+__device__ void amr_update(const StageArgs &a, const Sched &sched, unsigned int *ctr,
+                           unsigned long long &dtmin) {
+  const PackDev &p = a.p;
+  const double beta_dt = a.beta * a.ctl->dt;
+  for (int it = sched.first(ctr, a.ncell_items); it < a.ncell_items; it = sched.next(ctr, a.ncell_items, it)) {
+    const int2 w = a.cell_items[it];
+    const StepBlock &B = a.blocks[w.x];
+    const long long c = (long long)w.y + threadIdx.x;
+    if (c >= B.ncell) continue;
+    int i, j, k;
+    if (!is_interior(p, B, c, i, j, k)) continue;
+    const long long nc = B.ncell;
+    const long long ic = (long long)(j - p.ng) * B.nx[0] + (i - p.ng);
+    const double vol = B.dx[0] * B.dx[1] * B.dx[2];
+    double u[NHYDRO];
+#pragma unroll
+    for (int v = 0; v < NHYDRO; ++v) {
+      const double div = -B.du[v * B.nint + ic] / vol;
+      u[v] = a.gam0 * B.u0[v * nc + c] + a.gam1 * B.u1[v * nc + c] + beta_dt * div;
+    }
+    if (a.gravity) {
+      const double rho = B.prim[IDN * nc + c];
+      u[IM1] += a.grav[0] * rho * beta_dt;
+      double de = a.grav[0] * B.prim[IV1 * nc + c];
+      u[IM2] += a.grav[1] * rho * beta_dt;
+      de += a.grav[1] * B.prim[IV2 * nc + c];
+      u[IEN] += de * rho * beta_dt;
+    }
+#pragma unroll
+    for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + c] = u[v];
+    if (a.last) {
+      double wv[NHYDRO], gcc, gce;
+      cons_to_prim_cell(u, wv, gcc, gce, p.gm1, p.dfloor, p.pfloor);
+      const unsigned long long b = dt_bits(dt_candidate(wv, u[IEN], B.dx, p.ndim, p.gm1));
+      dtmin = b < dtmin ? b : dtmin;
+    }
+  }
+}
+
 template <int RECON, int RS>
 __global__ void __launch_bounds__(kStageThreads, 1) k_stage(StageArgs a) {
   extern __shared__ double sm[];
@@ -426,7 +504,13 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_stage(StageArgs a) {
     const int2 w = a.cell_items[it];
     const StepBlock &B = a.blocks[w.x];
     const long long c = (long long)w.y + threadIdx.x;
-    if (c < B.ncell) ghost_cell(a, B, c);
+    if (c < B.ncell) {
+      if (p.amr)
+        amr_fill_cell(a.blocks, B, [](const StepBlock &X) -> const double * { return X.u0; },
+                      p.bc, p.ng, c);
+      else
+        ghost_cell(a, B, c);
+    }
   }
   if (!a.init)
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < p.nblocks; b += gridDim.x * blockDim.x)
@@ -498,6 +582,12 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_stage(StageArgs a) {
         pass_item<3, RECON, RS>(a, B, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin);
     }
     if (!last_pass && !grid_barrier(a.ctl, a.timeout_ns)) return;
+  }
+  if (p.amr) {
+    if (!grid_barrier(a.ctl, a.timeout_ns)) return;
+    amr_correct(a, sched, ctr + 6);
+    if (!grid_barrier(a.ctl, a.timeout_ns)) return;
+    amr_update(a, sched, ctr + 7, dtmin);
   }
   if (a.last) {
     dtmin = block_min(dtmin);

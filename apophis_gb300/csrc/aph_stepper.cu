@@ -100,6 +100,10 @@ struct aph_stepper_s {
   int ncell_items = 0;
   int2 *d_line_items[3] = {nullptr, nullptr, nullptr};
   int nline_items[3] = {0, 0, 0};
+  int *d_fix_items = nullptr;   // refined meshes: blocks with a finer neighbour
+  int nfix_items = 0;
+  double *d_bflux = nullptr;
+  int bflux_stride = 0;
   int T[3] = {0, 0, 0};
   aph_stepper_config cfg;
   int grid = 0;
@@ -226,6 +230,9 @@ StageArgs stage_args(aph_stepper s, int stage_idx, const Stage &st, bool last, b
   a.init = init;
   a.schedule = s->cfg.schedule;
   a.timeout_ns = 4000000000ULL;
+  a.fix_items = s->d_fix_items;
+  a.nfix_items = s->nfix_items;
+  a.bflux_stride = s->bflux_stride;
   return a;
 }
 
@@ -317,6 +324,8 @@ void free_all(aph_stepper s) {
   cudaFree(s->d_ctl);
   cudaFree(s->d_cell_items);
   for (int d = 0; d < 3; ++d) cudaFree(s->d_line_items[d]);
+  cudaFree(s->d_fix_items);
+  cudaFree(s->d_bflux);
 }
 
 }  // namespace
@@ -334,8 +343,26 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
     return fail(APH_ERR_INVALID, "integrator %d not recognized", desc->integrator);
   if (desc->nblocks <= 0 || !desc->blocks) return fail(APH_ERR_INVALID, "no blocks");
   const int ndim = desc->params.ndim;
-  if ((long long)desc->nb[0] * desc->nb[1] * desc->nb[2] != desc->nblocks)
+  const bool amr = desc->amr != nullptr;
+  if (amr) {
+    if (ndim != 2) return fail(APH_ERR_UNSUPPORTED, "refined meshes are 2D");
+    std::vector<AmrFaces> faces(desc->nblocks);
+    std::vector<int> nxs(2 * desc->nblocks);
+    for (int b = 0; b < desc->nblocks; ++b) {
+      std::memcpy(&faces[b], &desc->amr[b], sizeof(AmrFaces));
+      nxs[2 * b] = desc->blocks[b].nx[0];
+      nxs[2 * b + 1] = desc->blocks[b].nx[1];
+    }
+    char msg[160];
+    if (amr_check(desc->nblocks, faces.data(), (const int(*)[2])nxs.data(), desc->params.nghost,
+                  msg, sizeof(msg)))
+      return fail(APH_ERR_INVALID, "%s", msg);
+    for (int f = 0; f < 4; ++f)
+      if (desc->bc[f] < 0 || desc->bc[f] > 2)
+        return fail(APH_ERR_INVALID, "boundary condition %d not recognized", desc->bc[f]);
+  } else if ((long long)desc->nb[0] * desc->nb[1] * desc->nb[2] != desc->nblocks) {
     return fail(APH_ERR_INVALID, "nb product != nblocks");
+  }
   aph_stepper s = new aph_stepper_s();
   s->params = desc->params;
   s->integrator = desc->integrator;
@@ -350,8 +377,9 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   p.pfloor = desc->params.pfloor;
   p.cfl = desc->params.cfl;
   fill_gas_consts(p);
+  p.amr = amr ? 1 : 0;
   for (int d = 0; d < 3; ++d) {
-    if (d >= ndim && desc->nb[d] != 1) {
+    if (!amr && d >= ndim && desc->nb[d] != 1) {
       delete s;
       return fail(APH_ERR_INVALID, "nb%d must be 1", d + 1);
     }
@@ -375,7 +403,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
         delete s;
         return fail(APH_ERR_INVALID, "block %d: nx%d invalid", b, d + 1);
       }
-      if (a.nx[d] != desc->blocks[0].nx[d]) {
+      if (!amr && a.nx[d] != desc->blocks[0].nx[d]) {
         delete s;
         return fail(APH_ERR_UNSUPPORTED, "a block grid with ghost exchange needs equal blocks");
       }
@@ -397,13 +425,19 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
     B.nk = ndim >= 3 ? a.nx[2] + 2 * p.ng : 1;
     B.ncell = (long long)B.ni * B.nj * B.nk;
     B.nint = (long long)a.nx[0] * a.nx[1] * a.nx[2];
-    B.loc[0] = b % p.nb[0];
-    B.loc[1] = (b / p.nb[0]) % p.nb[1];
-    B.loc[2] = b / (p.nb[0] * p.nb[1]);
+    if (amr) {
+      static_assert(sizeof(AmrFaces) == sizeof(aph_amr_block), "face table layout");
+      std::memcpy(&B.amr, &desc->amr[b], sizeof(AmrFaces));
+    } else {
+      B.loc[0] = b % p.nb[0];
+      B.loc[1] = (b / p.nb[0]) % p.nb[1];
+      B.loc[2] = b / (p.nb[0] * p.nb[1]);
+    }
     cells += B.ncell;
     inter += B.nint;
   }
-  for (int d = 0; d < 3; ++d) p.mesh_nx[d] = p.nb[d] * s->hblocks[0].nx[d];
+  if (!amr)
+    for (int d = 0; d < 3; ++d) p.mesh_nx[d] = p.nb[d] * s->hblocks[0].nx[d];
   s->total_cells = cells;
   s->total_interior = inter;
   s->gravity = desc->use_gravity != 0;
@@ -425,6 +459,23 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   ck(cudaMalloc(&s->d_flags, sizeof(int) * p.nblocks));
   ck(cudaMalloc(&s->d_ctl, sizeof(StepCtl)));
   ck(cudaMalloc(&s->d_blocks, sizeof(StepBlock) * p.nblocks));
+  if (amr) {
+    s->bflux_stride = 5 * std::max(p.max_nx[0], p.max_nx[1]);
+    ck(cudaMalloc(&s->d_bflux, sizeof(double) * 4 * s->bflux_stride * p.nblocks));
+    std::vector<int> fix;
+    for (int b = 0; b < p.nblocks; ++b)
+      for (int f = 0; f < 4; ++f)
+        if (desc->amr[b].face_kind[f] == APH_FACE_FINER) {
+          fix.push_back(b);
+          break;
+        }
+    s->nfix_items = (int)fix.size();
+    if (!fix.empty()) {
+      ck(cudaMalloc(&s->d_fix_items, sizeof(int) * fix.size()));
+      if (e == cudaSuccess)
+        e = cudaMemcpy(s->d_fix_items, fix.data(), sizeof(int) * fix.size(), cudaMemcpyHostToDevice);
+    }
+  }
   if (e != cudaSuccess) {
     free_all(s);
     delete s;
@@ -437,6 +488,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
     B.prim = s->d_prim + 5 * oc;
     B.gamma = s->d_gamma + 2 * oc;
     B.du = s->d_du + 5 * oi;
+    if (amr) B.bflux = s->d_bflux + (size_t)4 * s->bflux_stride * b;
     oc += B.ncell;
     oi += B.nint;
   }

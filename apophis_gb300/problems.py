@@ -95,6 +95,31 @@ def kh2d(n=512, block=64, ng=2, recon="plm", rsolver="hlle", integrator="rk2", c
     return cfg, cons
 
 
+def kh2d_smooth(n=512, block=64, ng=2, recon="plm", rsolver="hlle", integrator="rk2", cfl=0.3,
+                gamma=5.0 / 3.0, width=0.05):
+    """2D Kelvin-Helmholtz with resolved (tanh) shear layers at y = 0.25 and 0.75 and smooth
+    perturbations in every field, periodic unit square (the profile family of kh.cpp's
+    iprob=4).  No region is exactly flat, so the step is differentiable almost everywhere
+    (a piecewise-constant state puts every flat cell on a kink of the PLM limiter)."""
+    cfg = MeshConfig(ndim=2, mesh_nx=(n, n, 1), block_nx=(block, block, 1), ng=ng,
+                     recon=recon, rsolver=rsolver, integrator=integrator, cfl=cfl, gamma=gamma,
+                     name="kh2d_smooth")
+    cons = _alloc(cfg)
+    # layer positions and phases off the grid's symmetry lines: a profile mirrored about a
+    # cell face gives pairs of equal cells, i.e. zero differences sitting on the limiter's kink
+    y1, y2 = 0.25 + 0.0123, 0.75 + 0.0123
+    for b in range(cfg.nblocks):
+        x, y, _ = cfg.cell_centers(b)
+        band = 0.5 * (np.tanh((y - y1) / width) - np.tanh((y - y2) / width))
+        rho = 1.5 + 0.5 * band + 0.05 * np.sin(2.0 * math.pi * (x + 2.0 * y) + 0.37)
+        vx = band - 0.5 + 0.02 * np.cos(2.0 * math.pi * (2.0 * x - y) + 1.13)
+        vy = (0.01 * np.sin(4.0 * math.pi * x + 0.71) +
+              0.005 * np.sin(2.0 * math.pi * (x + y) + 2.29))
+        p = 2.5 + 0.05 * np.cos(2.0 * math.pi * (x - 3.0 * y) + 0.53)
+        _set_prim(cfg, cons, b, rho, vx, vy, 0.0, p)
+    return cfg, cons
+
+
 def rt2d(nx=256, ny=768, block=(32, 32), ng=4, recon="ppm", rsolver="hllc", integrator="rk2",
          cfl=0.4, gamma=1.4, g=-0.1):
     """2D Rayleigh-Taylor on [0,0.5]x[0,1.5]: rho 2 above rho 1, hydrostatic pressure

@@ -75,6 +75,21 @@ typedef struct aph_hydro_params {
                       shared reciprocals (about 1e-15 relative per operation) */
 } aph_hydro_params;
 
+/* Neighbours of one meshblock of a statically refined 2D mesh.  Levels differ by at most
+ * one across a face; periodic faces name the wrapped neighbour.  The Parthenon counterpart
+ * is the mesh's neighbour-block list used by its boundary communication. */
+#define APH_FACE_SAME 0      /* one neighbour on the same level */
+#define APH_FACE_COARSER 1   /* one neighbour one level coarser */
+#define APH_FACE_FINER 2     /* the neighbours one level finer that cover the face */
+#define APH_FACE_BOUNDARY 3  /* physical outflow / reflecting boundary */
+typedef struct aph_amr_block {
+  int level;           /* 0 = base level; cell width is the base width / 2^level */
+  int origin[2];       /* global index of the first interior cell, in cells of this level */
+  int face_kind[4];    /* faces x-, x+, y-, y+ */
+  int face_count[4];   /* neighbours across each face (up to 4 for APH_FACE_FINER) */
+  int face_nbr[4][4];  /* neighbour block indices, in transverse order */
+} aph_amr_block;
+
 /* A pack: the device-resident descriptor of a list of meshblocks (MeshData). */
 typedef struct aph_pack_s *aph_pack;
 
@@ -90,6 +105,20 @@ aph_status aph_pack_create(const aph_hydro_params *params, const aph_block *bloc
  * physical boundaries bc[2*d + side] (side 0 inner, 1 outer); needed by
  * aph_hydro_fill_ghosts. */
 aph_status aph_pack_set_topology(aph_pack pack, const int nb[3], const int bc[6]);
+/* Blocks form a statically refined 2D mesh (ndim 2, nvar 5): ghost fill uses the face
+ * tables (copy, 2x2 restriction, minmod-linear prolongation) and the flux-divergence update
+ * corrects coarse cells at coarse-fine faces to the mean of the fine face fluxes (the
+ * flux-correction tasks of apophis_driver.cpp:68, 74-76). bc as in aph_pack_set_topology. */
+aph_status aph_pack_set_amr(aph_pack pack, const aph_amr_block *amr, const int bc[6]);
+/* Host-only check of a refined mesh's face tables against the blocks' interior sizes
+ * nx[2*b], nx[2*b+1] (the check aph_pack_set_amr and aph_stepper_create run): kinds and
+ * counts in range, neighbours on the stated level and covering the whole face, coarse-fine
+ * faces on even cell boundaries, at least 2*nghost cells per side.  No device work. */
+aph_status aph_amr_check(const aph_amr_block *amr, const int *nx, int nblocks, int nghost);
+/* A partition of a pack: blocks first..first+count-1, sharing the parent's descriptors (and
+ * so its neighbours), for launches over part of a pack (one meshblock at a time, or one of
+ * Parthenon's pack partitions).  Destroy it before the parent. */
+aph_status aph_pack_partition(aph_pack parent, int first, int count, aph_pack *out);
 aph_status aph_pack_destroy(aph_pack pack);
 
 /* ConsToPrim<EOS_t> (src/hydro/hydro.cpp:422-533), the FillDerivedMesh callback:
@@ -168,6 +197,7 @@ typedef struct aph_stepper_desc {
   double gravity[3];
   double tlim;               /* parthenon/time/tlim; <= 0: none */
   double fixed_dt;           /* > 0: every step uses this dt instead of the CFL policy */
+  const aph_amr_block *amr;  /* NULL: uniform block grid (nb); else the refined 2D mesh */
 } aph_stepper_desc;
 
 /* Launch configuration, chosen by aph_stepper_autotune or set by hand. */

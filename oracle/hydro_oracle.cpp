@@ -674,6 +674,271 @@ static void step(Mesh &m, Real dt) {
   }
 }
 
+
+// ---- statically refined 2D mesh of uneven blocks -------------------------------------------
+// The multi-level counterpart of the boundary exchange + flux correction that Parthenon does
+// between levels (its prolongation/restriction and flux-correction code is not vendored,
+// parity of these semantics against the reference is unpinned).  Restated here exactly as
+// the CUDA path performs it:
+//  * ghost cells across a face come from the neighbours' interiors only: same level: copy;
+//    finer neighbour: average of the 2x2 fine cells, ((a+b)+(c+d))*0.25; coarser neighbour:
+//    minmod-limited linear prolongation c + o_n*s_n + o_t*s_t (o = +-1/4 by the fine cell's
+//    parity), s_n from the coarse neighbours along the normal (the one on the fine side is
+//    the restricted average of the fine block's own edge cells), s_t from the coarse
+//    block's transverse interior neighbours (0 at its edge); physical faces: outflow copy or
+//    reflecting mirror with the normal momentum negated; corner ghosts copy the nearest
+//    interior cell (no flux pass reads them);
+//  * conservation at coarse-fine faces: after the x and y flux differences are summed, the
+//    coarse boundary cell's difference is corrected from its own face flux F to the mean of
+//    the two fine face fluxes Fn: du += a*F - a*Fn on a low face, a*Fn - a*F on a high face,
+//    faces in the order x-, x+, y-, y+.
+enum { FACE_SAME = 0, FACE_COARSER = 1, FACE_FINER = 2, FACE_BOUNDARY = 3 };
+
+struct AmrBlock {
+  int level, origin[2], nx[2];
+  Real dx[3];
+  int kind[4], cnt[4], nbr[4][4];
+  Dims d;
+  size_t off;  // first cell of the block in the flat pack
+};
+
+struct AmrMesh {
+  int ng, recon, rsolver, integrator, bc[2][2], gravity;
+  Real gm1, cfl, dfloor, pfloor, g[3];
+  std::vector<AmrBlock> blocks;
+  size_t total = 0;
+  std::vector<Real> u0, u1, prim, gamma, flux[2], du;
+  std::vector<size_t> du_off;
+  Real time = 0, dt = 0;
+  int ncycle = 0;
+  int plant_no_correction = 0;  // tests only: skip the coarse-fine flux correction
+};
+
+static inline size_t ACELL(const AmrBlock &B, int d, int a, int t) {
+  // entire-domain cell of interior normal index a (along d) and transverse index t
+  const int i = d == 0 ? B.d.ng + a : B.d.ng + t;
+  const int j = d == 0 ? B.d.ng + t : B.d.ng + a;
+  return (size_t)j * B.d.ni + i;
+}
+static inline Real AU(const AmrMesh &m, const std::vector<Real> &q, const AmrBlock &B, int v,
+                      size_t cell) {
+  return q[B.off * 5 + (size_t)v * B.d.ncell + cell];
+}
+static inline Real minmod(Real a, Real b) {
+  if (!(a * b > 0.0)) return 0.0;
+  return (std::abs(a) < std::abs(b)) ? a : b;
+}
+
+// Ghost value of all 5 components for face (d, s) of block B at depth k, transverse index t.
+static void amr_ghost(const AmrMesh &m, const std::vector<Real> &q, const AmrBlock &B, int d,
+                      int s, int k, int t, Real *out) {
+  const int face = 2 * d + s, td = 1 - d;
+  const int kind = B.kind[face];
+  if (kind == FACE_SAME) {
+    const AmrBlock &N = m.blocks[B.nbr[face][0]];
+    const int a = s == 0 ? N.nx[d] - 1 - k : k;
+    const int tn = B.origin[td] + t - N.origin[td];
+    for (int v = 0; v < 5; ++v) out[v] = AU(m, q, N, v, ACELL(N, d, a, tn));
+  } else if (kind == FACE_BOUNDARY) {
+    const int bcv = m.bc[d][s];
+    if (bcv == BC_OUTFLOW) {
+      const int a = s == 0 ? 0 : B.nx[d] - 1;
+      for (int v = 0; v < 5; ++v) out[v] = AU(m, q, B, v, ACELL(B, d, a, t));
+    } else {
+      const int a = s == 0 ? k : B.nx[d] - 1 - k;
+      for (int v = 0; v < 5; ++v) {
+        const Real x = AU(m, q, B, v, ACELL(B, d, a, t));
+        out[v] = (v == 1 + d) ? -x : x;
+      }
+    }
+  } else if (kind == FACE_FINER) {
+    const int tg2 = 2 * (B.origin[td] + t);
+    const AmrBlock *F = nullptr;
+    for (int n = 0; n < B.cnt[face]; ++n) {
+      const AmrBlock &C = m.blocks[B.nbr[face][n]];
+      if (tg2 >= C.origin[td] && tg2 < C.origin[td] + C.nx[td]) F = &C;
+    }
+    const int ft = tg2 - F->origin[td];
+    const int a0 = s == 0 ? F->nx[d] - 1 - 2 * k : 2 * k;
+    const int a1 = s == 0 ? a0 - 1 : a0 + 1;
+    for (int v = 0; v < 5; ++v)
+      out[v] = ((AU(m, q, *F, v, ACELL(*F, d, a0, ft)) + AU(m, q, *F, v, ACELL(*F, d, a0, ft + 1))) +
+                (AU(m, q, *F, v, ACELL(*F, d, a1, ft)) + AU(m, q, *F, v, ACELL(*F, d, a1, ft + 1)))) *
+               0.25;
+  } else {  // COARSER
+    const AmrBlock &C = m.blocks[B.nbr[face][0]];
+    const int tg = B.origin[td] + t;
+    const int tc = (tg >> 1) - C.origin[td];
+    const int kc = k >> 1;
+    const int ic = s == 0 ? C.nx[d] - 1 - kc : kc;  // coarse normal index
+    // fine global normal index of the ghost and its coarse parent
+    const int gf = s == 0 ? B.origin[d] - 1 - k : B.origin[d] + B.nx[d] + k;
+    const Real on = (gf & 1) ? 0.25 : -0.25;
+    const Real ot = (tg & 1) ? 0.25 : -0.25;
+    for (int v = 0; v < 5; ++v) {
+      const Real c = AU(m, q, C, v, ACELL(C, d, ic, tc));
+      // neighbours along +d / -d in the coarse block's index space
+      Real cm, cp;
+      const int tf0 = 2 * (tc + C.origin[td]) - B.origin[td];  // fine transverse pair in B
+      auto restricted = [&](int a0, int a1) {
+        return ((AU(m, q, B, v, ACELL(B, d, a0, tf0)) + AU(m, q, B, v, ACELL(B, d, a0, tf0 + 1))) +
+                (AU(m, q, B, v, ACELL(B, d, a1, tf0)) + AU(m, q, B, v, ACELL(B, d, a1, tf0 + 1)))) *
+               0.25;
+      };
+      if (s == 0) {  // B lies on the +d side of C
+        cm = AU(m, q, C, v, ACELL(C, d, ic - 1, tc));
+        cp = ic + 1 < C.nx[d] ? AU(m, q, C, v, ACELL(C, d, ic + 1, tc)) : restricted(0, 1);
+      } else {       // B lies on the -d side of C
+        cm = ic - 1 >= 0 ? AU(m, q, C, v, ACELL(C, d, ic - 1, tc))
+                         : restricted(B.nx[d] - 1, B.nx[d] - 2);
+        cp = AU(m, q, C, v, ACELL(C, d, ic + 1, tc));
+      }
+      const Real sn = minmod(c - cm, cp - c);
+      Real st = 0.0;
+      if (tc - 1 >= 0 && tc + 1 < C.nx[td])
+        st = minmod(c - AU(m, q, C, v, ACELL(C, d, ic, tc - 1)), AU(m, q, C, v, ACELL(C, d, ic, tc + 1)) - c);
+      out[v] = c + on * sn + ot * st;
+    }
+  }
+}
+
+static void amr_fill_ghosts(AmrMesh &m, std::vector<Real> &q) {
+  // reads interiors only, writes ghosts only
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int b = 0; b < (int)m.blocks.size(); ++b) {
+    const AmrBlock &B = m.blocks[b];
+    const Dims &d = B.d;
+    Real val[5];
+    for (int j = 0; j < d.nj; ++j)
+      for (int i = 0; i < d.ni; ++i) {
+        const bool gi = i < d.ng || i >= d.ng + B.nx[0];
+        const bool gj = j < d.ng || j >= d.ng + B.nx[1];
+        if (!gi && !gj) continue;
+        const size_t cell = (size_t)j * d.ni + i;
+        if (gi && gj) {
+          const int ci = std::min(std::max(i, d.ng), d.ng + B.nx[0] - 1);
+          const int cj = std::min(std::max(j, d.ng), d.ng + B.nx[1] - 1);
+          for (int v = 0; v < 5; ++v) val[v] = AU(m, q, B, v, (size_t)cj * d.ni + ci);
+        } else if (gi) {
+          const int s = i < d.ng ? 0 : 1;
+          const int k = s == 0 ? d.ng - 1 - i : i - (d.ng + B.nx[0]);
+          amr_ghost(m, q, B, 0, s, k, j - d.ng, val);
+        } else {
+          const int s = j < d.ng ? 0 : 1;
+          const int k = s == 0 ? d.ng - 1 - j : j - (d.ng + B.nx[1]);
+          amr_ghost(m, q, B, 1, s, k, i - d.ng, val);
+        }
+        for (int v = 0; v < 5; ++v) q[B.off * 5 + (size_t)v * d.ncell + cell] = val[v];
+      }
+  }
+}
+
+static void amr_fill_derived(AmrMesh &m) {
+  for (const AmrBlock &B : m.blocks)
+    cons_to_prim(B.d, &m.u0[B.off * 5], &m.prim[B.off * 5], &m.gamma[B.off * 2], m.gm1, m.dfloor, m.pfloor);
+}
+
+static Real amr_estimate_dt(AmrMesh &m) {
+  Real mn = std::numeric_limits<Real>::max();
+  for (AmrBlock &B : m.blocks)
+    mn = std::min(mn, m.cfl * estimate_timestep_min(B.d, &m.prim[B.off * 5], &m.u0[B.off * 5], B.dx, m.gm1));
+  return mn;
+}
+
+static void amr_step(AmrMesh &m, Real dt) {
+  const int ns = nstages(m.integrator);
+  for (int stage = 1; stage <= ns; ++stage) {
+    if (stage == 1) m.u1 = m.u0;
+    Real gam0, gam1, beta;
+    stage_coeffs(m.integrator, stage, gam0, gam1, beta);
+    const int recon = (m.integrator == INT_VL2 && stage == 1) ? RECON_DC : m.recon;
+    const int nb = (int)m.blocks.size();
+    for (int b = 0; b < nb; ++b) {
+      AmrBlock &B = m.blocks[b];
+      calculate_fluxes(B.d, recon, m.rsolver, &m.prim[B.off * 5], &m.gamma[B.off * 2],
+                       &m.flux[0][B.off * 5], &m.flux[1][B.off * 5], nullptr);
+    }
+    // flux differences, x then y
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int b = 0; b < nb; ++b) {
+      AmrBlock &B = m.blocks[b];
+      const Dims &d = B.d;
+      const Real a1 = B.dx[1] * B.dx[2], a2 = B.dx[0] * B.dx[2];
+      const Real *F1 = &m.flux[0][B.off * 5], *F2 = &m.flux[1][B.off * 5];
+      Real *du = &m.du[m.du_off[b]];
+      const size_t nint = (size_t)B.nx[0] * B.nx[1];
+      for (int v = 0; v < 5; ++v)
+        for (int j = 0; j < B.nx[1]; ++j)
+          for (int i = 0; i < B.nx[0]; ++i) {
+            const size_t c = IX(d, v, 0, j + d.ng, i + d.ng);
+            Real x = (a1 * F1[c + 1] - a1 * F1[c]);
+            x += (a2 * F2[c + d.ni] - a2 * F2[c]);
+            du[v * nint + (size_t)j * B.nx[0] + i] = x;
+          }
+    }
+    // conservation at coarse-fine faces
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int b = 0; b < nb; ++b) {
+      AmrBlock &B = m.blocks[b];
+      Real *du = &m.du[m.du_off[b]];
+      const size_t nint = (size_t)B.nx[0] * B.nx[1];
+      for (int face = 0; face < 4; ++face) {
+        if (B.kind[face] != FACE_FINER || m.plant_no_correction) continue;
+        const int d = face / 2, s = face % 2, td = 1 - d;
+        const Real area = d == 0 ? B.dx[1] * B.dx[2] : B.dx[0] * B.dx[2];
+        const Real *Fb = &m.flux[d][B.off * 5];
+        for (int t = 0; t < B.nx[td]; ++t) {
+          const int tg2 = 2 * (B.origin[td] + t);
+          const AmrBlock *F = nullptr;
+          for (int n = 0; n < B.cnt[face]; ++n) {
+            const AmrBlock &C = m.blocks[B.nbr[face][n]];
+            if (tg2 >= C.origin[td] && tg2 < C.origin[td] + C.nx[td]) F = &C;
+          }
+          const int ft = tg2 - F->origin[td];
+          const Real *Ff = &m.flux[d][F->off * 5];
+          // face index (along d) of the shared face in each block
+          const int fb = s == 0 ? 0 : B.nx[d];
+          const int ff = s == 0 ? F->nx[d] : 0;
+          const int a = s == 0 ? 0 : B.nx[d] - 1;  // coarse boundary cell
+          for (int v = 0; v < 5; ++v) {
+            auto fidx = [&](const AmrBlock &X, int fa, int tt) {
+              const int i = d == 0 ? X.d.ng + fa : X.d.ng + tt;
+              const int j = d == 0 ? X.d.ng + tt : X.d.ng + fa;
+              return (size_t)v * X.d.ncell + (size_t)j * X.d.ni + i;
+            };
+            const Real Fold = Fb[fidx(B, fb, t)];
+            const Real Fnew = 0.5 * (Ff[fidx(*F, ff, ft)] + Ff[fidx(*F, ff, ft + 1)]);
+            const int i = d == 0 ? a : t, j = d == 0 ? t : a;
+            Real &x = du[v * nint + (size_t)j * B.nx[0] + i];
+            x = s == 0 ? x + (area * Fold - area * Fnew) : x + (area * Fnew - area * Fold);
+          }
+        }
+      }
+    }
+    // update, gravity
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int b = 0; b < nb; ++b) {
+      AmrBlock &B = m.blocks[b];
+      const Dims &d = B.d;
+      const Real vol = B.dx[0] * B.dx[1] * B.dx[2];
+      const Real *du = &m.du[m.du_off[b]];
+      const size_t nint = (size_t)B.nx[0] * B.nx[1];
+      Real *u0 = &m.u0[B.off * 5];
+      const Real *u1 = &m.u1[B.off * 5];
+      for (int v = 0; v < 5; ++v)
+        for (int j = 0; j < B.nx[1]; ++j)
+          for (int i = 0; i < B.nx[0]; ++i) {
+            const size_t c = IX(d, v, 0, j + d.ng, i + d.ng);
+            const Real div = -du[v * nint + (size_t)j * B.nx[0] + i] / vol;
+            u0[c] = gam0 * u0[c] + gam1 * u1[c] + beta * dt * div;
+          }
+      if (m.gravity) apply_gravity(d, u0, &m.prim[B.off * 5], m.g, beta * dt);
+    }
+    amr_fill_ghosts(m, m.u0);
+    amr_fill_derived(m);
+  }
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -787,6 +1052,80 @@ int orc_mesh_run(void *h, int nsteps, double tlim, double fixed_dt) {
 
 void orc_mesh_state(void *h, double *out3) {
   Mesh &m = *(Mesh *)h;
+  out3[0] = m.time; out3[1] = m.dt; out3[2] = m.ncycle;
+}
+
+
+// ---- refined mesh driver ------------------------------------------------------------------
+// ints: [nblocks, ng, recon, rsolver, integrator, bc x1i, x1o, x2i, x2o, gravity]
+// blk (per block 1+2+2+4+4+16 = 29 ints): level, origin[2], nx[2], kind[4], cnt[4], nbr[4][4]
+// reals: [gm1, cfl, dfloor, pfloor, g1, g2, g3]; bdx: per block dx1, dx2, dx3
+void *orc_amr_create(const int *ints, const int *blk, const double *reals, const double *bdx) {
+  AmrMesh *m = new AmrMesh();
+  const int nb = ints[0];
+  m->ng = ints[1]; m->recon = ints[2]; m->rsolver = ints[3]; m->integrator = ints[4];
+  m->bc[0][0] = ints[5]; m->bc[0][1] = ints[6]; m->bc[1][0] = ints[7]; m->bc[1][1] = ints[8];
+  m->gravity = ints[9];
+  m->gm1 = reals[0]; m->cfl = reals[1]; m->dfloor = reals[2]; m->pfloor = reals[3];
+  for (int d = 0; d < 3; ++d) m->g[d] = reals[4 + d];
+  m->blocks.resize(nb);
+  size_t off = 0, doff = 0;
+  for (int b = 0; b < nb; ++b) {
+    AmrBlock &B = m->blocks[b];
+    const int *p = blk + 29 * b;  // level, origin[2], nx[2], kind[4], cnt[4], nbr[4][4]
+    B.level = p[0]; B.origin[0] = p[1]; B.origin[1] = p[2]; B.nx[0] = p[3]; B.nx[1] = p[4];
+    for (int f = 0; f < 4; ++f) { B.kind[f] = p[5 + f]; B.cnt[f] = p[9 + f]; }
+    for (int f = 0; f < 4; ++f) for (int n = 0; n < 4; ++n) B.nbr[f][n] = p[13 + 4 * f + n];
+    for (int d = 0; d < 3; ++d) B.dx[d] = bdx[3 * b + d];
+    B.d = make_dims(5, B.nx[0], B.nx[1], 1, m->ng, 2);
+    B.off = off;
+    off += B.d.ncell;
+    m->du_off.push_back(doff);
+    doff += (size_t)5 * B.nx[0] * B.nx[1];
+  }
+  m->total = off;
+  m->u0.assign(5 * off, 0.0); m->u1.assign(5 * off, 0.0); m->prim.assign(5 * off, 0.0);
+  m->gamma.assign(2 * off, 0.0); m->flux[0].assign(5 * off, 0.0); m->flux[1].assign(5 * off, 0.0);
+  m->du.assign(doff, 0.0);
+  return m;
+}
+
+void orc_amr_destroy(void *h) { delete (AmrMesh *)h; }
+
+// Plants a mistake for the tests: the step skips the coarse-fine flux correction.
+void orc_amr_plant_no_correction(void *h) { ((AmrMesh *)h)->plant_no_correction = 1; }
+
+void orc_amr_set_cons(void *h, const double *cons) {
+  AmrMesh &m = *(AmrMesh *)h;
+  std::memcpy(m.u0.data(), cons, m.u0.size() * sizeof(double));
+  amr_fill_ghosts(m, m.u0);
+  amr_fill_derived(m);
+  m.dt = amr_estimate_dt(m);
+}
+
+void orc_amr_get(void *h, int what, double *out) {
+  AmrMesh &m = *(AmrMesh *)h;
+  const std::vector<Real> &v = what == 0 ? m.u0 : m.prim;
+  std::memcpy(out, v.data(), v.size() * sizeof(double));
+}
+
+int orc_amr_run(void *h, int nsteps, double tlim, double fixed_dt) {
+  AmrMesh &m = *(AmrMesh *)h;
+  int taken = 0;
+  while (taken < nsteps && m.time < tlim) {
+    Real dt = fixed_dt > 0 ? fixed_dt : m.dt;
+    if (fixed_dt <= 0 && (tlim - m.time) < dt) dt = tlim - m.time;
+    amr_step(m, dt);
+    m.time += dt;
+    m.ncycle++;
+    taken++;
+    m.dt = std::min(2.0 * dt, amr_estimate_dt(m));
+  }
+  return taken;
+}
+
+void orc_amr_state(void *h, double *out3) {
+  AmrMesh &m = *(AmrMesh *)h;
   out3[0] = m.time; out3[1] = m.dt; out3[2] = m.ncycle;
 }
 

@@ -159,3 +159,64 @@ class Mesh:
         out = np.zeros(3)
         lib().orc_mesh_state(self.h, _p(out))
         return {"time": out[0], "dt": out[1], "ncycle": int(out[2])}
+
+
+class AmrMesh:
+    """Statically refined 2D mesh (apophis_gb300.amr.AmrConfig) driven by the oracle."""
+
+    def __init__(self, cfg):
+        self.cfg = cfg
+        bc = cfg.bc
+        ints = [cfg.nblocks, cfg.ng, RECON[cfg.recon], RSOLVER[cfg.rsolver],
+                INTEGRATOR[cfg.integrator], BC[bc[0][0]], BC[bc[0][1]], BC[bc[1][0]],
+                BC[bc[1][1]], 1 if cfg.gravity is not None else 0]
+        blk = []
+        bdx = []
+        for B in cfg.blocks:
+            row = [B.level, B.origin[0], B.origin[1], B.nx[0], B.nx[1]]
+            row += list(B.face_kind) + [len(n) for n in B.face_nbr]
+            for n in B.face_nbr:
+                row += list(n) + [0] * (4 - len(n))
+            blk += row
+            bdx += [B.dx[0], B.dx[1], 1.0]
+        g = cfg.gravity if cfg.gravity is not None else (0.0, 0.0, 0.0)
+        reals = [cfg.gm1, cfg.cfl, cfg.dfloor, cfg.pfloor, *g]
+        L = lib()
+        L.orc_amr_create.restype = ctypes.c_void_p
+        L.orc_amr_create.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _dp, _dp]
+        L.orc_amr_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_amr_set_cons.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_amr_get.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
+        L.orc_amr_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_amr_run.restype = ctypes.c_int
+        L.orc_amr_state.argtypes = [ctypes.c_void_p, _dp]
+        self._keep = [(ctypes.c_int * len(ints))(*ints), (ctypes.c_int * len(blk))(*blk),
+                      (ctypes.c_double * len(reals))(*reals), (ctypes.c_double * len(bdx))(*bdx)]
+        self.h = L.orc_amr_create(*self._keep)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_amr_destroy(self.h)
+            self.h = None
+
+    def set_cons(self, cons):
+        c = np.ascontiguousarray(cons, dtype=np.float64)
+        assert c.size == self.cfg.flat_size(5)
+        lib().orc_amr_set_cons(self.h, _p(c))
+
+    def get(self, what="cons"):
+        out = np.empty(self.cfg.flat_size(5))
+        lib().orc_amr_get(self.h, 0 if what == "cons" else 1, _p(out))
+        return out
+
+    def plant_no_correction(self):
+        """Tests only: make the oracle skip the coarse-fine flux correction."""
+        lib().orc_amr_plant_no_correction(ctypes.c_void_p(self.h))
+
+    def run(self, nsteps=1 << 30, tlim=1e300, fixed_dt=0.0):
+        return lib().orc_amr_run(self.h, int(nsteps), ctypes.c_double(tlim), ctypes.c_double(fixed_dt))
+
+    def state(self):
+        out = np.zeros(3)
+        lib().orc_amr_state(self.h, _p(out))
+        return {"time": out[0], "dt": out[1], "ncycle": int(out[2])}

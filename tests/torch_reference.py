@@ -40,7 +40,7 @@ def _recon(q, recon, axis):
     sl = lambda a, b: q.narrow(axis, a + 2, b - a)  # cells a..b-1
     if recon == "dc":
         return sl(-1, n), sl(0, n + 1)
-    qm, q0, qp = sl(-2, n + 1), sl(-1, n + 2), sl(0, n + 3)  # around cells -1..n
+    qm, q0, qp = sl(-2, n), sl(-1, n + 1), sl(0, n + 2)  # around cells -1..n
     dql = q0 - qm
     dqr = qp - q0
     dq2 = dql * dqr
