@@ -324,9 +324,11 @@ aph_status aph_pack_partition(aph_pack parent, int first, int count, aph_pack *o
   parent->children++;
   p->uniform = parent->uniform;
   p->has_topology = parent->has_topology;
+  for (int d = 0; d < 3; ++d) p->dev.max_nx[d] = 0;
   for (const BlockDev &B : p->host_blocks) {
     p->max_ncell = std::max<long long>(p->max_ncell, B.ncell);
     p->max_interior = std::max(p->max_interior, B.nx[0] * B.nx[1] * B.nx[2]);
+    for (int d = 0; d < 3; ++d) p->dev.max_nx[d] = std::max(p->dev.max_nx[d], B.nx[d]);
   }
   cudaError_t e = cudaMalloc(&p->d_scratch, 4 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&p->d_dt, 2 * sizeof(double));

@@ -321,17 +321,49 @@ __global__ void __launch_bounds__(kThreads) k_apply_gravity(PackDev p, const Blo
 // ---------------------------------------------------------------------------------------
 static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
+// Launch shapes.  FP64 issue is a per-SM resource (a few lanes per clock), so a launch
+// that covers few SMs -- one small meshblock at a time -- is bound by the latency of its
+// longest thread.  Small launches therefore use fewer threads (or lines) per CTA, down to
+// one warp, until the grid spans about two CTAs per SM; launches over a whole pack keep the
+// full CTA.  The arithmetic of every cell is the same for any shape.
+static int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (!cached[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+    cached[dev] = n;
+  }
+  return cached[dev];
+}
+
+static int launch_threads(long long work, int nblocks) {
+  const long long want = 2LL * sm_count();
+  int t = kThreads;
+  while (t > 32 && (long long)cdiv(work, t) * nblocks < want) t >>= 1;
+  return t;
+}
+
 cudaError_t launch_cons_to_prim(const PackDev &p, const BlockDev *blocks, int max_ncell,
                                 int *floor_flag, cudaStream_t s) {
-  dim3 grid(cdiv(max_ncell, kThreads), p.nblocks);
-  k_cons_to_prim<<<grid, kThreads, 0, s>>>(p, blocks, floor_flag);
+  const int nt = launch_threads(max_ncell, p.nblocks);
+  dim3 grid(cdiv(max_ncell, nt), p.nblocks);
+  k_cons_to_prim<<<grid, nt, 0, s>>>(p, blocks, floor_flag);
   return cudaGetLastError();
 }
 
 template <int DIR, int RECON, int RS>
 static cudaError_t launch_fluxes_t(const PackDev &p, const BlockDev *blocks, cudaStream_t s) {
   const int n = p.max_nx[DIR - 1];
-  const int T = (n + 2 >= kThreads) ? 1 : kThreads / (n + 2);
+  long long ntrans;
+  if (DIR == 1) ntrans = (long long)p.max_nx[1] * p.max_nx[2];
+  else if (DIR == 2) ntrans = (long long)p.max_nx[0] * p.max_nx[2];
+  else ntrans = (long long)p.max_nx[0] * p.max_nx[1];
+  int T = (n + 2 >= kThreads) ? 1 : kThreads / (n + 2);
+  while (T > 1 && (long long)cdiv(ntrans, T) * p.nblocks < 2LL * sm_count()) T = (T + 1) / 2;
+  const int nt = (int)std::min<long long>(kThreads, 32LL * cdiv((long long)T * (n + 2), 32));
   const int V = p.nvar + 2;
   const size_t smem = (size_t)2 * V * T * (n + 2) * sizeof(double);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
@@ -342,12 +374,8 @@ static cudaError_t launch_fluxes_t(const PackDev &p, const BlockDev *blocks, cud
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  long long ntrans;
-  if (DIR == 1) ntrans = (long long)p.max_nx[1] * p.max_nx[2];
-  else if (DIR == 2) ntrans = (long long)p.max_nx[0] * p.max_nx[2];
-  else ntrans = (long long)p.max_nx[0] * p.max_nx[1];
   dim3 grid(cdiv(ntrans, T), p.nblocks);
-  k_fluxes<DIR, RECON, RS><<<grid, kThreads, smem, s>>>(p, blocks, T);
+  k_fluxes<DIR, RECON, RS><<<grid, nt, smem, s>>>(p, blocks, T);
   return cudaGetLastError();
 }
 
@@ -384,26 +412,29 @@ cudaError_t launch_fluxes(const PackDev &p, const BlockDev *blocks, int dir, int
 cudaError_t launch_update(const PackDev &p, const BlockDev *blocks, double gam0, double gam1,
                           double beta, double beta_dt_host, const double *dt_dev,
                           int max_interior, cudaStream_t s) {
-  dim3 grid(cdiv(max_interior, kThreads), p.nblocks);
+  const int nt = launch_threads(max_interior, p.nblocks);
+  dim3 grid(cdiv(max_interior, nt), p.nblocks);
   if (p.amr)
-    k_update_amr<<<grid, kThreads, 0, s>>>(p, blocks, gam0, gam1, beta, beta_dt_host, dt_dev);
+    k_update_amr<<<grid, nt, 0, s>>>(p, blocks, gam0, gam1, beta, beta_dt_host, dt_dev);
   else
-    k_update<<<grid, kThreads, 0, s>>>(p, blocks, gam0, gam1, beta, beta_dt_host, dt_dev);
+    k_update<<<grid, nt, 0, s>>>(p, blocks, gam0, gam1, beta, beta_dt_host, dt_dev);
   return cudaGetLastError();
 }
 
 cudaError_t launch_estimate_dt(const PackDev &p, const BlockDev *blocks, int max_interior,
                                unsigned long long *min_bits, cudaStream_t s) {
-  dim3 grid(cdiv(max_interior, kThreads), p.nblocks);
-  k_estimate_dt<<<grid, kThreads, 0, s>>>(p, blocks, min_bits);
+  const int nt = launch_threads(max_interior, p.nblocks);
+  dim3 grid(cdiv(max_interior, nt), p.nblocks);
+  k_estimate_dt<<<grid, nt, 0, s>>>(p, blocks, min_bits);
   return cudaGetLastError();
 }
 
 cudaError_t launch_apply_gravity(const PackDev &p, const BlockDev *blocks, double g0, double g1,
                                  double g2, double beta, double beta_dt_host,
                                  const double *dt_dev, int max_interior, cudaStream_t s) {
-  dim3 grid(cdiv(max_interior, kThreads), p.nblocks);
-  k_apply_gravity<<<grid, kThreads, 0, s>>>(p, blocks, g0, g1, g2, beta, beta_dt_host, dt_dev);
+  const int nt = launch_threads(max_interior, p.nblocks);
+  dim3 grid(cdiv(max_interior, nt), p.nblocks);
+  k_apply_gravity<<<grid, nt, 0, s>>>(p, blocks, g0, g1, g2, beta, beta_dt_host, dt_dev);
   return cudaGetLastError();
 }
 

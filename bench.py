@@ -16,12 +16,21 @@ roofline  HBM roofline of the stage kernel with the algorithmic 200 B per zone-u
 cpu_baseline  the oracle (C++ FP64 restatement of the reference's CPU path) on the host
         cores, a bounded sample of the same workload.
 
+amr     the uneven refined pack (2D Rayleigh-Taylor, 256 x 768 base grid, two static levels:
+        1440 meshblocks of 32^2 and 16^2, PPM+HLLC, RK2, gravity): the batched stepper
+        against the plain per-pack and per-meshblock launch paths (the latter host-driven,
+        and replayed from a CUDA graph as its best case).
+adjoint the adjoint/forward time ratio on the differentiable rollout (2D KH 512^2 as 64
+        blocks of 64^2, PLM+HLLE, RK2, checkpoint every 20 steps): reverse sweep (with
+        recomputation) per step over the batched forward step.
+
 --impl reference times that CPU path alone (all host threads) on the same workload.
 Under torchrun (N > 1) every rank runs its own replica of the workload (the hydro step
 shards by meshblocks, but this build drives one GPU per replica and exchanges nothing);
 the step time is the max over ranks.
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -137,6 +146,127 @@ def cpu_baseline(cfg, cons, nsteps, threads=None):
     return cfg.zones() * nsteps / el, O.num_threads(), el
 
 
+def amr_leg(args, warmup):
+    """The uneven refined pack: batched stepper vs the plain launch paths (rank 0)."""
+    import torch
+    from apophis_gb300 import amr, hydro
+    cfg, cons = amr.rt2d_amr()
+    zones = cfg.zones()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def timed(fn, n):
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record()
+        fn(n)
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / n
+
+    st = amr.AmrStepper(cfg, cons, exact=False)
+    tune = None if args.no_tune else st.autotune(trial_steps=2)
+    st.step(warmup)
+    st.status()
+    stage_ms = st.profile(nsteps=2)
+    nsteps = 100
+    bms = timed(st.step, nsteps)
+    status = st.status()
+    st.close()
+    out = {"workload": "rt2d_amr: 1440 meshblocks (160 of 32^2 at level 0, 256 + 1024 of 16^2 "
+                       "at levels 1-2), 491,520 zones, PPM+HLLC, RK2, gravity -0.1, FP64",
+           "batched": {"value": zones / (bms * 1e-3), "ms_per_step": bms, "steps": nsteps,
+                       "stage_ms": stage_ms, "launches_per_step": 3,
+                       "launch": tune["config"] if tune else None, "sim_time": status["time"]}}
+    drv = amr.AmrDriver(cfg, cons, exact=False)
+    drv.run(nsteps=2)
+    pms = timed(lambda n: drv.run(nsteps=n), 20)
+    out["plain_per_pack"] = {"value": zones / (pms * 1e-3), "ms_per_step": pms}
+    drv.md.close()
+    del drv
+    # per meshblock, host-driven: each kernel launched once per block through the C ABI
+    drv = amr.AmrDriver(cfg, cons, exact=False, per_block=True)
+    drv.run(nsteps=1)
+    hms = timed(lambda n: drv.run(nsteps=n), 2)
+    # the same launches replayed from one CUDA graph (no host cost): fixed dt, each block's
+    # dt estimate written to the device
+    dts = torch.empty(cfg.nblocks, dtype=torch.float64, device="cuda")
+    from apophis_gb300 import _capi
+
+    def body():
+        drv.step(1e-5)
+        for b, p in enumerate(drv.md.block_packs):
+            _capi.call("aph_hydro_estimate_timestep_async", p,
+                       ctypes.c_void_p(dts.data_ptr() + 8 * b), hydro.stream_handle())
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        body()
+    torch.cuda.current_stream().wait_stream(side)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        body()
+    g.replay()
+    gms = timed(lambda n: [g.replay() for _ in range(n)], 10)
+    launches = cfg.nblocks * (2 * 5 + 3) + 2
+    out["plain_per_meshblock"] = {"value": zones / (hms * 1e-3), "ms_per_step": hms,
+                                  "launches_per_step": launches, "driver": "host (ctypes)"}
+    out["plain_per_meshblock_graph"] = {"value": zones / (gms * 1e-3), "ms_per_step": gms,
+                                        "launches_per_step": launches,
+                                        "driver": "one CUDA graph per step"}
+    del g
+    drv.md.close()
+    del drv
+    torch.cuda.empty_cache()
+    out["batched_vs_plain_per_meshblock_graph"] = gms / bms
+    out["batched_vs_plain_per_meshblock"] = hms / bms
+    out["batched_vs_plain_per_pack"] = pms / bms
+    bytes_per_launch = BYTES_PER_ZONE_UPDATE * zones / len(stage_ms)
+    out["hbm_achieved_gbs"] = bytes_per_launch / (sum(stage_ms) / len(stage_ms) * 1e-3) / 1e9
+    return out
+
+
+def adjoint_leg(nsteps=40):
+    """Adjoint/forward time ratio on the differentiable rollout (rank 0)."""
+    import torch
+    from apophis_gb300 import problems
+    from apophis_gb300.adjoint import Adjoint
+    from apophis_gb300.stepper import Stepper
+    cfg, cons = problems.kh2d(n=512, block=64, ng=2, recon="plm", rsolver="hlle")
+    u0 = torch.from_numpy(cons).cuda()
+    adj = Adjoint(cfg)
+    dts = [2e-4] * nsteps
+    adj.forward(u0, dts[:4], 2)
+    adj.backward(torch.ones_like(u0))
+    torch.cuda.synchronize()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    a, b, c = ev(), ev(), ev()
+    a.record()
+    uT = adj.forward(u0, dts, 20)
+    b.record()
+    adj.backward(torch.ones_like(uT))
+    c.record()
+    torch.cuda.synchronize()
+    fwd_tape = a.elapsed_time(b) / nsteps
+    bwd = b.elapsed_time(c) / nsteps
+    adj.close()
+    st = Stepper(cfg, cons, exact=False, fixed_dt=2e-4)
+    st.autotune(trial_steps=1)
+    st.step(3)
+    st.status()
+    a, b = ev(), ev()
+    a.record()
+    st.step(nsteps)
+    b.record()
+    torch.cuda.synchronize()
+    fwd = a.elapsed_time(b) / nsteps
+    st.close()
+    return {"workload": "kh2d 512^2 (64 blocks of 64^2), PLM+HLLE, RK2, %d steps, checkpoint "
+                        "every 20" % nsteps,
+            "forward_ms_per_step": fwd, "checkpointed_forward_ms_per_step": fwd_tape,
+            "backward_ms_per_step": bwd, "ratio": bwd / fwd,
+            "note": "backward includes the recomputation of each checkpoint segment"}
+
+
 def run_reference(args, cfg, cons):
     dist, rank, ws = dist_init()
     if rank != 0:
@@ -163,6 +293,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-meshblock path")
+    ap.add_argument("--no-amr", action="store_true", help="skip the refined-pack leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint ratio leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -280,6 +412,11 @@ def main():
     if plain is not None:
         line["plain"] = plain
         line["batched_vs_plain"] = value / ws / plain["value"]
+    if rank == 0 and not args.no_amr:
+        line["amr"] = amr_leg(args, args.warmup)
+        line["gpu_launches_amr_batched_step"] = 3
+    if rank == 0 and not args.no_adjoint:
+        line["adjoint"] = adjoint_leg()
     if rank == 0 and not args.no_cpu:
         zps, cores, el = cpu_baseline(cfg, cons, 1)
         line["cpu_baseline"] = {"value": zps, "unit": UNIT, "cores": cores, "kind": "port",
