@@ -32,6 +32,7 @@ struct AdjGeom {
   int bc[3][2];
   double dx[3];
   GasConsts gc;
+  double ic2g;  // 1 / (C^2 gamma)
 };
 
 __host__ __device__ __forceinline__ long long blk_off(const AdjGeom &g, int b) {
@@ -74,6 +75,7 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
   double *GL = SR + 5 * T * W2;               // [5][T][W2]  adjoint of left state, face f
   double *GR = GL + 5 * T * W2;               // [5][T][W2]  adjoint of right state, face f
   double *CC = GR + 5 * T * W2;               // [3][5][T][W2] recon vjp contributions
+  double *RR = CC + 3 * 5 * T * W2;           // [5][T][W2]  PLM reciprocal per cell (0: flat)
   const double *P = prim + blk_off(g, b);
   const double *M = mu + blk_off(g, b);
   double *LW = lam_w + blk_off(g, b);
@@ -96,7 +98,7 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
   for (int it = tid; it < 5 * nl * W2; it += nth) {  // cells -1..n
     const int v = it / (nl * W2), r = it % (nl * W2), t = r / W2, c = r % W2 - 1;
     double ql, qr;
-    if (RECON == RECON_PLM) plm(q(v, t, c - 1), q(v, t, c), q(v, t, c + 1), ql, qr);
+    if (RECON == RECON_PLM) RR[(v * T + t) * W2 + c + 1] = plm_keep(q(v, t, c - 1), q(v, t, c), q(v, t, c + 1), ql, qr);
     else ql = qr = q(v, t, c);
     SL[(v * T + t) * W2 + c + 1] = ql;
     SR[(v * T + t) * W2 + c + 1] = qr;
@@ -117,8 +119,8 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
       const double mlo = f > 0 ? MU[(v * T + t) * n + f - 1] : 0.0;
       gf[k] = scale * (mhi - mlo);
     }
-    if (RS == RS_HLLE) hlle_vjp(wl, wr, g.gc, gf, gwl, gwr);
-    else hllc_vjp(wl, wr, g.gc, gf, gwl, gwr);
+    if (RS == RS_HLLE) hlle_vjp(wl, wr, g.gc, g.ic2g, gf, gwl, gwr);
+    else hllc_vjp(wl, wr, g.gc, g.ic2g, gf, gwl, gwr);
     for (int k = 0; k < 5; ++k) {
       GL[(perm[k] * T + t) * W2 + f] = gwl[k];
       GR[(perm[k] * T + t) * W2 + f] = gwr[k];
@@ -133,7 +135,7 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
     const double gR = c >= 0 ? GR[o + c] : 0.0;          // adjoint of qr_c
     double gm, g0, gp;
     if (RECON == RECON_PLM) {
-      plm_vjp(q(v, t, c - 1), q(v, t, c), q(v, t, c + 1), gL, gR, gm, g0, gp);
+      plm_vjp(q(v, t, c - 1), q(v, t, c), q(v, t, c + 1), RR[o + c + 1], gL, gR, gm, g0, gp);
     } else {
       gm = 0.0;
       g0 = gL + gR;
@@ -159,22 +161,26 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
 }
 
 // ---- ConsToPrim vjp over the entire domain ----------------------------------------------
-__global__ void k_c2p_vjp(AdjGeom g, const double *u, const double *lam_w, double *lam_u) {
+__global__ void k_c2p_vjp(AdjGeom g, const double *w, const double *lam_w, double *lam_u) {
   const int b = blockIdx.y;
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.ncell) return;
   const long long o = blk_off(g, b), nc = g.ncell;
-  double uu[5], gw[5], gu[5];
+  double ww[5], gw[5], gu[5];
   for (int v = 0; v < 5; ++v) {
-    uu[v] = u[o + v * nc + c];
+    ww[v] = w[o + v * nc + c];
     gw[v] = lam_w[o + v * nc + c];
   }
-  cons_to_prim_vjp(uu, gw, g.gc.gm1, gu);
+  cons_to_prim_vjp(ww, gw, g.gc.gm1, gu);
   for (int v = 0; v < 5; ++v) lam_u[o + v * nc + c] = gu[v];
 }
 
-// ---- ghost map transposed: each interior cell gathers the ghost copies made of it ---------
-__global__ void k_ghost_vjp(AdjGeom g, const double *lam_u, double *out) {
+// ---- ghost map transposed: each interior cell gathers the ghost copies made of it, giving
+// r = R'(u)^T mu; fused with the stage combination  acc += gam1 a;  a = gam0 a + r  (acc
+// starts at zero when acc_zero), and at the first stage with  lam_n = a + acc  (when lam_n is
+// given, a and acc are not stored).
+__global__ void k_ghost_vjp(AdjGeom g, const double *lam_u, double *a, double *acc_buf,
+                            double gam0, double gam1, int acc_zero, double *lam_n) {
   const int b = blockIdx.y;
   const int nint = g.nx[0] * g.nx[1] * g.nx[2];
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -225,7 +231,18 @@ __global__ void k_ghost_vjp(AdjGeom g, const double *lam_u, double *out) {
       }
     }
   }
-  for (int v = 0; v < 5; ++v) out[blk_off(g, b) + v * nc + self] = acc[v];
+  for (int v = 0; v < 5; ++v) {
+    const long long o = blk_off(g, b) + v * nc + self;
+    const double av = a[o];
+    const double cv = (acc_zero ? 0.0 : acc_buf[o]) + gam1 * av;
+    const double an = gam0 * av + acc[v];
+    if (lam_n) {
+      lam_n[o] = an + cv;
+    } else {
+      acc_buf[o] = cv;
+      a[o] = an;
+    }
+  }
 }
 
 // out = alpha * x + beta * y on interior cells (ghost entries of out set to zero)
@@ -266,7 +283,7 @@ struct aph_adjoint_s {
   int integrator = 0;
   size_t n = 0;  // doubles per pack field
   double *x = nullptr, *u1 = nullptr, *prim = nullptr, *gamma = nullptr, *flux[3] = {nullptr, nullptr, nullptr};
-  double *lam_w = nullptr, *lam_u = nullptr, *mu = nullptr, *r = nullptr, *a = nullptr, *acc = nullptr;
+  double *lam_w = nullptr, *lam_u = nullptr, *a = nullptr, *acc = nullptr;
   double *states = nullptr;  // per stage input of the step being differentiated
   int *floor_flag = nullptr;
   aph_pack pack = nullptr;
@@ -287,15 +304,16 @@ cudaError_t fwd_prepare(aph_adjoint A, cudaStream_t s) {
                                        A->floor_flag, s);
 }
 
-// One fixed-dt RK step of A->x (interior in, interior + ghosts + prim out); if keep, the
-// input of every stage is saved in A->states.
-aph_status fwd_step(aph_adjoint A, double dt, bool keep, cudaStream_t s) {
+// One fixed-dt RK step of A->x (interior in, interior + ghosts + prim out).  With keep
+// non-null the primitives of every stage input (entire domain) are saved there, one pack
+// field per stage.
+aph_status fwd_step(aph_adjoint A, double dt, double *keep, cudaStream_t s) {
   const std::vector<StageC> st = stages_for(A->integrator);
   cudaError_t e = fwd_prepare(A, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(A->u1, A->x, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   for (size_t i = 0; i < st.size() && e == cudaSuccess; ++i) {
     if (keep)
-      e = cudaMemcpyAsync(A->states + i * A->n, A->x, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      e = cudaMemcpyAsync(keep + i * A->n, A->prim, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) break;
     const int recon = (A->integrator == APH_INTEGRATOR_VL2 && i == 0) ? APH_RECON_DC : A->params.recon;
     if (aph_hydro_calculate_fluxes(A->pack, recon, A->params.rsolver, s) != APH_OK) return APH_ERR_CUDA;
@@ -307,12 +325,14 @@ aph_status fwd_step(aph_adjoint A, double dt, bool keep, cudaStream_t s) {
 }
 
 template <int DIR>
-cudaError_t launch_pass(aph_adjoint A, int recon, double scale, cudaStream_t s) {
+cudaError_t launch_pass(aph_adjoint A, int recon, double scale, const double *prim_in,
+                        cudaStream_t s) {
   const AdjGeom &g = A->g;
   const int n = g.nx[DIR - 1];
   const int T = std::max(1, 256 / (n + 2));
   const int G = recon == APH_RECON_PLM ? 2 : 1;
-  const size_t smem = sizeof(double) * (5 * T * (n + 2 * G) + 5 * T * n + 4 * 5 * T * (n + 2) + 3 * 5 * T * (n + 2));
+  const size_t smem = sizeof(double) * (5 * T * (n + 2 * G) + 5 * T * n + 4 * 5 * T * (n + 2) +
+                                        3 * 5 * T * (n + 2) + 5 * T * (n + 2));
   const int ntrans = DIR == 1 ? g.nx[1] * g.nx[2] : DIR == 2 ? g.nx[0] * g.nx[2] : g.nx[0] * g.nx[1];
   dim3 grid((ntrans + T - 1) / T, g.nblocks);
   const void *k = nullptr;
@@ -325,77 +345,73 @@ cudaError_t launch_pass(aph_adjoint A, int recon, double scale, cudaStream_t s) 
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   AdjGeom gg = g;
-  const double *prim = A->prim;
-  const double *mu = A->mu;
+  const double *prim = prim_in;
+  const double *mu = A->a;
   double *lw = A->lam_w;
   int TT = T;
   void *args[] = {&gg, &prim, &mu, &lw, &scale, &TT};
   return cudaLaunchKernel(k, grid, dim3(256), args, smem, s);
 }
 
-// r = R'(u)^T (beta dt a) for the state in A->x (ghosts filled, prim current)
-cudaError_t stage_vjp(aph_adjoint A, int recon, double bdt, cudaStream_t s) {
+// R'(u)^T (beta dt a) for the stage input whose primitives (entire domain, ghosts included)
+// are prim, combined into a / acc (k_ghost_vjp).
+cudaError_t stage_vjp(aph_adjoint A, int recon, double bdt, const double *prim, double gam0,
+                      double gam1, bool acc_zero, double *lam_n, cudaStream_t s) {
   const AdjGeom &g = A->g;
   const unsigned gx = (unsigned)((g.ncell + 255) / 256);
   cudaError_t e = cudaMemsetAsync(A->lam_w, 0, A->n * sizeof(double), s);
-  // mu = beta dt a
-  if (e == cudaSuccess) {
-    k_axpby<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, bdt, A->a, 0.0, nullptr, A->mu);
-    e = cudaGetLastError();
-  }
   const double vol = g.dx[0] * g.dx[1] * g.dx[2];
   const double area[3] = {g.dx[1] * g.dx[2], g.dx[0] * g.dx[2], g.dx[0] * g.dx[1]};
   for (int d = 1; d <= g.ndim && e == cudaSuccess; ++d) {
-    const double scale = area[d - 1] / vol;
-    e = d == 1 ? launch_pass<1>(A, recon, scale, s) : d == 2 ? launch_pass<2>(A, recon, scale, s)
-                                                             : launch_pass<3>(A, recon, scale, s);
+    const double scale = bdt * (area[d - 1] / vol);  // mu = beta dt a
+    e = d == 1 ? launch_pass<1>(A, recon, scale, prim, s)
+               : d == 2 ? launch_pass<2>(A, recon, scale, prim, s) : launch_pass<3>(A, recon, scale, prim, s);
   }
   if (e == cudaSuccess) {
-    k_c2p_vjp<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, A->x, A->lam_w, A->lam_u);
+    k_c2p_vjp<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, prim, A->lam_w, A->lam_u);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
     const int nint = g.nx[0] * g.nx[1] * g.nx[2];
-    k_ghost_vjp<<<dim3((nint + 255) / 256, g.nblocks), 256, 0, s>>>(g, A->lam_u, A->r);
+    k_ghost_vjp<<<dim3((nint + 255) / 256, g.nblocks), 256, 0, s>>>(g, A->lam_u, A->a, A->acc, gam0,
+                                                                   gam1, acc_zero ? 1 : 0, lam_n);
     e = cudaGetLastError();
   }
   return e;
 }
 
-// lam_n = (d U^{n+1} / d U^n)^T lam_next for the step from u_n with dt.
-aph_status step_vjp(aph_adjoint A, const double *u_n, double dt, const double *lam_next,
-                    double *lam_n, cudaStream_t s) {
+// lam_n = (d U^{n+1} / d U^n)^T lam_next for the step whose stage inputs' primitives (as
+// fwd_step keeps them: one pack field per stage) are `kept`, with dt.  lam_n may alias
+// lam_next.
+aph_status step_vjp_kept(aph_adjoint A, const double *kept, double dt, const double *lam_next,
+                         double *lam_n, cudaStream_t s) {
   const std::vector<StageC> st = stages_for(A->integrator);
   const AdjGeom &g = A->g;
   const unsigned gx = (unsigned)((g.ncell + 255) / 256);
-  cudaError_t e = cudaMemcpyAsync(A->x, u_n, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(e, "adjoint step");
-  if (aph_status r = fwd_step(A, dt, true, s)) return r;
   k_axpby<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, 1.0, lam_next, 0.0, nullptr, A->a);
-  k_axpby<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, 0.0, lam_next, 0.0, nullptr, A->acc);
-  for (int i = (int)st.size() - 1; i >= 0 && e == cudaSuccess; --i) {
-    e = cudaMemcpyAsync(A->x, A->states + i * A->n, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) break;
-    e = fwd_prepare(A, s);  // prim of this stage's input
+  cudaError_t e = cudaGetLastError();
+  const int ns = (int)st.size();
+  for (int i = ns - 1; i >= 0 && e == cudaSuccess; --i) {
     const int recon = (A->integrator == APH_INTEGRATOR_VL2 && i == 0) ? APH_RECON_DC : A->params.recon;
-    if (e == cudaSuccess) e = stage_vjp(A, recon, st[i].beta * dt, s);
-    if (e != cudaSuccess) break;
-    // acc += gam1 a ; a = gam0 a + r
-    k_axpby<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, 1.0, A->acc, st[i].gam1, A->a, A->acc);
-    k_axpby<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, st[i].gam0, A->a, 1.0, A->r, A->a);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) {
-    k_axpby<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, 1.0, A->a, 1.0, A->acc, lam_n);
-    e = cudaGetLastError();
+    e = stage_vjp(A, recon, st[i].beta * dt, kept + (size_t)i * A->n, st[i].gam0, st[i].gam1,
+                  i == ns - 1, i == 0 ? lam_n : nullptr, s);
   }
   return e == cudaSuccess ? APH_OK : cuda_fail(e, "adjoint step");
+}
+
+// The same from the step's input u_n: recompute the step, keeping its stage inputs.
+aph_status step_vjp(aph_adjoint A, const double *u_n, double dt, const double *lam_next,
+                    double *lam_n, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyAsync(A->x, u_n, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint step");
+  if (aph_status r = fwd_step(A, dt, A->states, s)) return r;
+  return step_vjp_kept(A, A->states, dt, lam_next, lam_n, s);
 }
 
 void adj_free(aph_adjoint A) {
   if (A->pack) aph_pack_destroy(A->pack);
   double *bufs[] = {A->x, A->u1, A->prim, A->gamma, A->flux[0], A->flux[1], A->flux[2], A->lam_w,
-                    A->lam_u, A->mu, A->r, A->a, A->acc, A->states, A->ckpts};
+                    A->lam_u, A->a, A->acc, A->states, A->ckpts};
   for (double *p : bufs) cudaFree(p);
   cudaFree(A->floor_flag);
 }
@@ -452,12 +468,13 @@ aph_status aph_adjoint_create(const aph_stepper_desc *desc, aph_adjoint *out) {
   tmp.gm1 = q.gm1;
   fill_gas_consts(tmp);
   g.gc = GasConsts{tmp.gm1, tmp.igm1, tmp.gamma, tmp.c2g, tmp.one_igm1, tmp.hlle_k, tmp.hllc_k};
+  g.ic2g = 1.0 / tmp.c2g;
   A->n = (size_t)g.nblocks * 5 * g.ncell;
   const size_t bytes = A->n * sizeof(double);
   const int ns = (int)stages_for(A->integrator).size();
   cudaError_t e = cudaSuccess;
   auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-  double **bufs[] = {&A->x, &A->u1, &A->prim, &A->lam_w, &A->lam_u, &A->mu, &A->r, &A->a, &A->acc};
+  double **bufs[] = {&A->x, &A->u1, &A->prim, &A->lam_w, &A->lam_u, &A->a, &A->acc};
   for (double **b : bufs) ck(cudaMalloc(b, bytes));
   ck(cudaMalloc(&A->gamma, bytes / 5 * 2));
   for (int d = 0; d < g.ndim; ++d) ck(cudaMalloc(&A->flux[d], bytes));
@@ -511,7 +528,7 @@ aph_status aph_adjoint_step(aph_adjoint A, const double *u_n, double dt, double 
   cudaMemsetAsync(A->floor_flag, 0, sizeof(int), s);
   cudaError_t e = cudaMemcpyAsync(A->x, u_n, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint forward");
-  if (aph_status st = fwd_step(A, dt, false, s)) return st;
+  if (aph_status st = fwd_step(A, dt, nullptr, s)) return st;
   e = cudaMemcpyAsync(u_next, A->x, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint forward");
   return check_floor(A, s);
@@ -550,7 +567,7 @@ aph_status aph_adjoint_forward(aph_adjoint A, const double *u0, int nsteps, cons
       e = cudaMemcpyAsync(A->ckpts + (size_t)(k / checkpoint_every) * A->n, A->x, A->n * sizeof(double),
                           cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) break;
-    if (aph_status st = fwd_step(A, dts[k], false, s)) return st;
+    if (aph_status st = fwd_step(A, dts[k], nullptr, s)) return st;
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(u_final, A->x, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint rollout");
@@ -564,21 +581,22 @@ aph_status aph_adjoint_backward(aph_adjoint A, const double *lam_final, double *
   if (A->dts.empty()) return fail(APH_ERR_INVALID, "no recorded rollout");
   cudaStream_t s = (cudaStream_t)stream;
   const int nsteps = (int)A->dts.size(), K = A->ckpt_every;
-  // segment storage: the state at the start of each step of one segment
+  const int ns = (int)stages_for(A->integrator).size();
+  // segment storage: the stage inputs of every step of one segment, recomputed once from the
+  // segment's checkpoint
   double *seg = nullptr;
-  cudaError_t e = cudaMalloc(&seg, (size_t)K * A->n * sizeof(double));
+  const size_t per_step = (size_t)ns * A->n;
+  cudaError_t e = cudaMalloc(&seg, (size_t)K * per_step * sizeof(double));
   if (e != cudaSuccess) return cuda_fail(e, "segment allocation");
   e = cudaMemcpyAsync(lam_initial, lam_final, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   aph_status st = APH_OK;
   for (int j = A->nckpt - 1; j >= 0 && st == APH_OK && e == cudaSuccess; --j) {
     const int k0 = j * K, k1 = std::min(nsteps, k0 + K);
     e = cudaMemcpyAsync(A->x, A->ckpts + (size_t)j * A->n, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    for (int k = k0; k < k1 && st == APH_OK && e == cudaSuccess; ++k) {
-      e = cudaMemcpyAsync(seg + (size_t)(k - k0) * A->n, A->x, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-      if (e == cudaSuccess && k + 1 < k1) st = fwd_step(A, A->dts[k], false, s);
-    }
+    for (int k = k0; k < k1 && st == APH_OK && e == cudaSuccess; ++k)
+      st = fwd_step(A, A->dts[k], seg + (size_t)(k - k0) * per_step, s);
     for (int k = k1 - 1; k >= k0 && st == APH_OK && e == cudaSuccess; --k)
-      st = step_vjp(A, seg + (size_t)(k - k0) * A->n, A->dts[k], lam_initial, lam_initial, s);
+      st = step_vjp_kept(A, seg + (size_t)(k - k0) * per_step, A->dts[k], lam_initial, lam_initial, s);
   }
   if (e == cudaSuccess && st == APH_OK) e = cudaStreamSynchronize(s);
   cudaFree(seg);

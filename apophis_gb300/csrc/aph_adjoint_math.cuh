@@ -15,11 +15,11 @@
 namespace aph {
 
 // ---- ConsToPrim: W = (rho, m/rho, p = gm1 (E - |m|^2 / (2 rho))) -----------------------
-__device__ __forceinline__ void cons_to_prim_vjp(const double *u, const double *gw, double gm1,
+// The Jacobian depends on rho and v only, so it is evaluated from the primitives w.
+__device__ __forceinline__ void cons_to_prim_vjp(const double *w, const double *gw, double gm1,
                                                  double *gu) {
-  const double rho = u[IDN];
-  const double di = 1.0 / rho;
-  const double v1 = u[IM1] * di, v2 = u[IM2] * di, v3 = u[IM3] * di;
+  const double di = 1.0 / w[IDN];
+  const double v1 = w[IV1], v2 = w[IV2], v3 = w[IV3];
   const double gp = gw[IPR];
   const double v2sum = v1 * v1 + v2 * v2 + v3 * v3;
   gu[IDN] = gw[IDN] - (gw[IV1] * v1 + gw[IV2] * v2 + gw[IV3] * v3) * di + gp * 0.5 * gm1 * v2sum;
@@ -29,20 +29,34 @@ __device__ __forceinline__ void cons_to_prim_vjp(const double *u, const double *
   gu[IEN] = gp * gm1;
 }
 
-// ---- PLM (plm_simple.hpp:15-32): gL is the adjoint of ql_{i+1}, gR of qr_i ------------
-__device__ __forceinline__ void plm_vjp(double q_im1, double q_i, double q_ip1, double gL,
-                                        double gR, double &g_im1, double &g_i, double &g_ip1) {
+// ---- PLM (plm_simple.hpp:15-32) ---------------------------------------------------------
+// Forward with the reciprocal kept: dqm = dq2 r, r = 1/(dql + dqr) where the slopes agree in
+// sign, r = 0 where the limiter returns 0.
+__device__ __forceinline__ double plm_keep(double q_im1, double q_i, double q_ip1, double &ql,
+                                           double &qr) {
   const double dql = q_i - q_im1, dqr = q_ip1 - q_i;
   const double dq2 = dql * dqr;
+  double r = 0.0, dqm = 0.0;
+  if (is_pos(dq2)) {
+    r = 1.0 / (dql + dqr);
+    dqm = dq2 * r;
+  }
+  ql = q_i + dqm;
+  qr = q_i - dqm;
+  return r;
+}
+
+// gL is the adjoint of ql_{i+1}, gR of qr_i; r as plm_keep returned it.
+__device__ __forceinline__ void plm_vjp(double q_im1, double q_i, double q_ip1, double r, double gL,
+                                        double gR, double &g_im1, double &g_i, double &g_ip1) {
   g_i = gL + gR;
   g_im1 = 0.0;
   g_ip1 = 0.0;
-  if (is_pos(dq2)) {
-    const double s = dql + dqr;
-    const double is2 = 1.0 / (s * s);
-    const double gm = gL - gR;                 // adjoint of dqm
-    const double gdql = gm * dqr * dqr * is2;  // d dqm / d dql = dqr^2 / s^2
-    const double gdqr = gm * dql * dql * is2;  // d dqm / d dqr = dql^2 / s^2
+  if (r != 0.0) {
+    const double dql = q_i - q_im1, dqr = q_ip1 - q_i;
+    const double gr2 = (gL - gR) * r * r;  // adjoint of dqm times 1/(dql + dqr)^2
+    const double gdql = gr2 * dqr * dqr;   // d dqm / d dql = dqr^2 / s^2
+    const double gdqr = gr2 * dql * dql;   // d dqm / d dqr = dql^2 / s^2
     g_i += gdql - gdqr;
     g_im1 = -gdql;
     g_ip1 = gdqr;
@@ -50,28 +64,31 @@ __device__ __forceinline__ void plm_vjp(double q_im1, double q_i, double q_ip1, 
 }
 
 // ---- sound speed c = sqrt(N/D), N = C^2 gamma p, D = p (1 + 1/gm1) + rho C^2 ------------
+// ip = 1/p; 1/D = c^2 / N = c^2 ip / (C^2 gamma), so no division beyond ip.
 struct SoundSpeed {
   double c, dc_dp, dc_drho;
 };
-__device__ __forceinline__ SoundSpeed sound_speed_d(double rho, double p, const GasConsts &gc) {
+__device__ __forceinline__ SoundSpeed sound_speed_d(double rho, double p, double ip,
+                                                    const GasConsts &gc, double ic2g) {
   const double N = gc.c2g * p;
   const double D = fma(p, gc.one_igm1, rho * C_LIGHT2);
   const double c = N * rsqrt(N * D);
-  const double iD = 1.0 / D;
+  const double iD = c * c * ip * ic2g;
   SoundSpeed s;
   s.c = c;
-  s.dc_dp = 0.5 * c * (1.0 / p - gc.one_igm1 * iD);
+  s.dc_dp = 0.5 * c * (ip - gc.one_igm1 * iD);
   s.dc_drho = -0.5 * c * C_LIGHT2 * iD;
   return s;
 }
 
 // ---- HLLE (hydro_hlle.hpp:28-133) ----------------------------------------------------------
 // w*: (rho, v_n, v_t1, v_t2, p); gf: adjoint of the 5 flux components; gwl/gwr: output.
-__device__ void hlle_vjp(const double *wl, const double *wr, const GasConsts &gc,
+__device__ void hlle_vjp(const double *wl, const double *wr, const GasConsts &gc, double ic2g,
                          const double *gf, double *gwl, double *gwr) {
   const double igm1 = gc.igm1;
-  const SoundSpeed sl = sound_speed_d(wl[IDN], wl[IPR], gc);
-  const SoundSpeed sr = sound_speed_d(wr[IDN], wr[IPR], gc);
+  const double ipl = 1.0 / wl[IPR], ipr = 1.0 / wr[IPR];
+  const SoundSpeed sl = sound_speed_d(wl[IDN], wl[IPR], ipl, gc, ic2g);
+  const SoundSpeed sr = sound_speed_d(wr[IDN], wr[IPR], ipr, gc, ic2g);
   const double cl = sl.c, cr = sr.c;
   const double kel = wl[IV1] * wl[IV1] + wl[IV2] * wl[IV2] + wl[IV3] * wl[IV3];
   const double ker = wr[IV1] * wr[IV1] + wr[IV2] * wr[IV2] + wr[IV3] * wr[IV3];
@@ -82,8 +99,8 @@ __device__ void hlle_vjp(const double *wl, const double *wr, const GasConsts &gc
   const double pmid = .5 * (wl[IPR] + wr[IPR] + (wl[IV1] - wr[IV1]) * rhoa * ca);
   const bool bl = gt(pmid, wl[IPR]), br = gt(pmid, wr[IPR]);
   const double k = gc.hlle_k;
-  const double ql = bl ? 1.0 + k * (pmid / wl[IPR] - 1.0) : 1.0;
-  const double qr = br ? 1.0 + k * (pmid / wr[IPR] - 1.0) : 1.0;
+  const double ql = bl ? 1.0 + k * (pmid * ipl - 1.0) : 1.0;
+  const double qr = br ? 1.0 + k * (pmid * ipr - 1.0) : 1.0;
   const double al = wl[IV1] - cl * ql;
   const double ar = wr[IV1] + cr * qr;
   const bool bpos = is_pos(ar), bneg = is_neg(al);
@@ -152,14 +169,12 @@ __device__ void hlle_vjp(const double *wl, const double *wr, const GasConsts &gc
   // ql, qr
   double gpmid = 0.0;
   if (bl) {
-    const double ip = 1.0 / wl[IPR];
-    gpmid += gql * k * ip;
-    gwl[IPR] -= gql * k * pmid * ip * ip;
+    gpmid += gql * k * ipl;
+    gwl[IPR] -= gql * k * pmid * ipl * ipl;
   }
   if (br) {
-    const double ip = 1.0 / wr[IPR];
-    gpmid += gqr * k * ip;
-    gwr[IPR] -= gqr * k * pmid * ip * ip;
+    gpmid += gqr * k * ipr;
+    gwr[IPR] -= gqr * k * pmid * ipr * ipr;
   }
   // pmid = 0.5 (pl + pr + (ul - ur) rhoa ca)
   gwl[IPR] += 0.5 * gpmid;
@@ -178,11 +193,12 @@ __device__ void hlle_vjp(const double *wl, const double *wr, const GasConsts &gc
 }
 
 // ---- HLLC (hydro_hllc.hpp:161-282) -----------------------------------------------------------
-__device__ void hllc_vjp(const double *wl, const double *wr, const GasConsts &gc,
+__device__ void hllc_vjp(const double *wl, const double *wr, const GasConsts &gc, double ic2g,
                          const double *gf, double *gwl, double *gwr) {
   const double igm1 = gc.igm1;
-  const SoundSpeed sdl = sound_speed_d(wl[IDN], wl[IPR], gc);
-  const SoundSpeed sdr = sound_speed_d(wr[IDN], wr[IPR], gc);
+  const double ipl = 1.0 / wl[IPR], ipr = 1.0 / wr[IPR];
+  const SoundSpeed sdl = sound_speed_d(wl[IDN], wl[IPR], ipl, gc, ic2g);
+  const SoundSpeed sdr = sound_speed_d(wr[IDN], wr[IPR], ipr, gc, ic2g);
   const double cl = sdl.c, cr = sdr.c;
   const double rl = wl[IDN], ul = wl[IV1], vl = wl[IV2], zl = wl[IV3], pl = wl[IPR];
   const double rr = wr[IDN], ur = wr[IV1], vr = wr[IV2], zr = wr[IV3], pr = wr[IPR];
@@ -194,10 +210,12 @@ __device__ void hllc_vjp(const double *wl, const double *wr, const GasConsts &gc
   const double pstar = .5 * (pl + pr) - .5 * (ur - ul) * rhoa * ca;
   const double k = gc.hllc_k;
   const bool bl = gt(pstar, pl), br = gt(pstar, pr);
-  const double argl = bl ? 1.0 + k * (pstar / pl - 1.0) : 1.0;
-  const double argr = br ? 1.0 + k * (pstar / pr - 1.0) : 1.0;
-  const double ql = bl ? sqrt(argl) : 1.0;
-  const double qr = br ? sqrt(argr) : 1.0;
+  const double argl = bl ? 1.0 + k * (pstar * ipl - 1.0) : 1.0;
+  const double argr = br ? 1.0 + k * (pstar * ipr - 1.0) : 1.0;
+  const double iql = bl ? rsqrt(argl) : 1.0;  // q = arg / sqrt(arg), 1/q kept for the reverse
+  const double iqr = br ? rsqrt(argr) : 1.0;
+  const double ql = bl ? argl * iql : 1.0;
+  const double qr = br ? argr * iqr : 1.0;
   const double sl = ul - cl * ql;
   const double sr = ur + cr * qr;
   const bool bpos = is_pos(sr), bneg = is_neg(sl);
@@ -315,16 +333,14 @@ __device__ void hllc_vjp(const double *wl, const double *wr, const GasConsts &gc
   // ql = sqrt(1 + k (pstar/pl - 1)) when pstar > pl
   double gpstar = 0.0;
   if (bl) {
-    const double garg = gql * 0.5 / ql;
-    const double ip = 1.0 / pl;
-    gpstar += garg * k * ip;
-    gwl[IPR] -= garg * k * pstar * ip * ip;
+    const double garg = gql * 0.5 * iql;
+    gpstar += garg * k * ipl;
+    gwl[IPR] -= garg * k * pstar * ipl * ipl;
   }
   if (br) {
-    const double garg = gqr * 0.5 / qr;
-    const double ip = 1.0 / pr;
-    gpstar += garg * k * ip;
-    gwr[IPR] -= garg * k * pstar * ip * ip;
+    const double garg = gqr * 0.5 * iqr;
+    gpstar += garg * k * ipr;
+    gwr[IPR] -= garg * k * pstar * ipr * ipr;
   }
   // pstar = 0.5 (pl + pr) - 0.5 (ur - ul) rhoa ca
   gwl[IPR] += 0.5 * gpstar;
