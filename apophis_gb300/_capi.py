@@ -36,13 +36,20 @@ class aph_amr_block(ctypes.Structure):
                 ("face_nbr", (ctypes.c_int * 4) * 4)]
 
 
+class aph_ensemble(ctypes.Structure):
+    _fields_ = [("nmembers", ctypes.c_int), ("member", ctypes.POINTER(ctypes.c_int)),
+                ("gm1", ctypes.POINTER(ctypes.c_double)),
+                ("tlim", ctypes.POINTER(ctypes.c_double))]
+
+
 class aph_stepper_desc(ctypes.Structure):
     _fields_ = [("params", aph_hydro_params), ("integrator", ctypes.c_int),
                 ("nblocks", ctypes.c_int), ("blocks", ctypes.POINTER(aph_block)),
                 ("nb", ctypes.c_int * 3), ("bc", ctypes.c_int * 6),
                 ("use_gravity", ctypes.c_int), ("gravity", ctypes.c_double * 3),
                 ("tlim", ctypes.c_double), ("fixed_dt", ctypes.c_double),
-                ("amr", ctypes.POINTER(aph_amr_block))]
+                ("amr", ctypes.POINTER(aph_amr_block)),
+                ("ensemble", ctypes.POINTER(aph_ensemble))]
 
 
 class aph_stepper_config(ctypes.Structure):
@@ -112,6 +119,8 @@ SIGNATURES = {
     "aph_stepper_step": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_status": ([ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int),
                             ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_member_status": ([ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int),
+                                   ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_get_config": ([ctypes.c_void_p, ctypes.POINTER(aph_stepper_config)],
                                ctypes.c_int),
     "aph_stepper_set_config": ([ctypes.c_void_p, ctypes.POINTER(aph_stepper_config)],

@@ -56,6 +56,7 @@ struct PackDev {
 struct StepBlock {
   double *u0, *u1, *prim, *gamma, *du;
   double *bflux;      // refined meshes: fluxes of the 4 boundary faces, [face][t][5]
+  int member;         // ensembles: the member (independent problem) the block belongs to
   int nx[3];
   int ni, nj, nk;
   int loc[3];
@@ -78,6 +79,16 @@ struct StepCtl {
   unsigned int work[8];         // dynamic work counters, one per phase
 };
 
+// One member of an ensemble (independent problems batched in one pack): its gas constants
+// (as PackDev's), its clock and its dt reduction.  active: time < tlim at the start of the
+// step; inactive members' blocks are skipped.
+struct MemberCtl {
+  double gm1, igm1, gamma, c2g, one_igm1, hlle_k, hllc_k;
+  double dt, time, tlim;
+  unsigned long long min_bits;
+  int ncycle, active;
+};
+
 // Arguments of one stage launch.
 struct StageArgs {
   PackDev p;
@@ -91,6 +102,8 @@ struct StageArgs {
   const int *fix_items;         // refined meshes: blocks with a finer neighbour
   int nfix_items;
   int bflux_stride;             // doubles per face of bflux (max transverse cells * 5)
+  int cf;                       // refined meshes with coarse-fine faces: correction phases
+  MemberCtl *members;           // ensembles (NULL: one problem, clock in ctl)
   int T[3];
   int order[3];                 // sweep order (1-based directions)
   double gam0, gam1, beta;

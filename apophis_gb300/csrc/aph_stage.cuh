@@ -181,6 +181,34 @@ __device__ __forceinline__ unsigned long long dt_bits(double m) {
   return is_neg(m) ? ~0ULL : (unsigned long long)__double_as_longlong(m);
 }
 
+// ---- ensembles: per-member gas constants, clock and dt minimum ---------------------------
+__device__ __forceinline__ GasConsts gas_of(const StageArgs &a, const StepBlock &B) {
+  if (a.members) {
+    const MemberCtl &m = a.members[B.member];
+    return GasConsts{m.gm1, m.igm1, m.gamma, m.c2g, m.one_igm1, m.hlle_k, m.hllc_k};
+  }
+  return GasConsts{a.p.gm1, a.p.igm1, a.p.gamma, a.p.c2g, a.p.one_igm1, a.p.hlle_k, a.p.hllc_k};
+}
+
+__device__ __forceinline__ bool active_of(const StageArgs &a, const StepBlock &B) {
+  return !a.members || a.members[B.member].active;
+}
+
+__device__ __forceinline__ double dt_of(const StageArgs &a, const StepBlock &B) {
+  return a.members ? a.members[B.member].dt : a.ctl->dt;
+}
+
+// Fold each thread's dt candidate into its member's minimum.  Called by whole warps whose
+// lanes all work on one block.
+__device__ __forceinline__ void member_min(const StageArgs &a, int member, unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, v, o);
+    v = x < v ? x : v;
+  }
+  if ((threadIdx.x & 31) == 0 && v != ~0ULL) atomicMin(&a.members[member].min_bits, v);
+}
+
 // ---- line geometry of a pass ----------------------------------------------------------
 // Line l of block B along DIR: the cell of interior position c on it is base + c*stride;
 // its interior index (for du) is ibase + c*istride.
@@ -232,6 +260,7 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
   constexpr int G = Halo<RECON>::G;
   const int n = B.nx[DIR - 1];
   const int V = constg ? 5 : 7;
+  const GasConsts gc = gas_of(a, B);
   const int NW = n + 2 * G;
   const long long nc = B.ncell;
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -317,7 +346,6 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
     constexpr int ivx = DIR;
     constexpr int ivy = IV1 + ((ivx - IV1) + 1) % 3;
     constexpr int ivz = IV1 + ((ivx - IV1) + 2) % 3;
-    const GasConsts gc{a.p.gm1, a.p.igm1, a.p.gamma, a.p.c2g, a.p.one_igm1, a.p.hlle_k, a.p.hllc_k};
     const int w2 = n + 2, w1 = n + 1;
     const size_t vs = (size_t)T * w2;
     for (int it = tid; it < nl * w1; it += nth) {
@@ -350,7 +378,7 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
     }
   }
   __syncthreads();
-  if (a.p.amr) {  // keep the boundary-face fluxes of every line for the coarse-fine correction
+  if (a.cf) {  // keep the boundary-face fluxes of every line for the coarse-fine correction
     const int w1 = n + 1;
     const size_t fs = (size_t)T * w1;
     for (int it = tid; it < nl * 2 * NHYDRO; it += nth) {
@@ -364,7 +392,7 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
     const int w1 = n + 1;
     const size_t fs = (size_t)T * w1;
     const double area = DIR == 1 ? B.dx[1] * B.dx[2] : DIR == 2 ? B.dx[0] * B.dx[2] : B.dx[0] * B.dx[1];
-    if (!last_pass || a.p.amr) {
+    if (!last_pass || a.cf) {
       for (int it = tid; it < NHYDRO * nl * n; it += nth) {
         const int v = it / (nl * n);
         const int r = it - v * nl * n;
@@ -378,7 +406,8 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
       }
     } else {
       const double vol = B.dx[0] * B.dx[1] * B.dx[2];
-      const double beta_dt = a.beta * a.ctl->dt;
+      const double beta_dt = a.beta * dt_of(a, B);
+      unsigned long long mymin = ~0ULL;
       for (int it = tid; it < nl * n; it += nth) {
         const int t = it / n, c = it - t * n;
         long long base, stride, ib, is;
@@ -412,10 +441,14 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
         for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + cell] = u[v];
         if (a.last) {  // EstimateTimestep on the floored new state
           double w[NHYDRO], gcc, gce;
-          cons_to_prim_cell(u, w, gcc, gce, a.p.gm1, a.p.dfloor, a.p.pfloor);
-          const unsigned long long b = dt_bits(dt_candidate(w, u[IEN], B.dx, a.p.ndim, a.p.gm1));
-          dtmin = b < dtmin ? b : dtmin;
+          cons_to_prim_cell(u, w, gcc, gce, gc.gm1, a.p.dfloor, a.p.pfloor);
+          const unsigned long long b = dt_bits(dt_candidate(w, u[IEN], B.dx, a.p.ndim, gc.gm1));
+          mymin = b < mymin ? b : mymin;
         }
+      }
+      if (a.last) {
+        if (a.members) member_min(a, B.member, mymin);
+        else dtmin = mymin < dtmin ? mymin : dtmin;
       }
     }
   }
@@ -503,6 +536,7 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_stage(StageArgs a) {
        it = sched.next(ctr + 0, a.ncell_items, it)) {
     const int2 w = a.cell_items[it];
     const StepBlock &B = a.blocks[w.x];
+    if (!active_of(a, B)) continue;
     const long long c = (long long)w.y + threadIdx.x;
     if (c < B.ncell) {
       if (p.amr)
@@ -522,23 +556,32 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_stage(StageArgs a) {
        it = sched.next(ctr + 1, a.ncell_items, it)) {
     const int2 w = a.cell_items[it];
     const StepBlock &B = a.blocks[w.x];
+    if (!active_of(a, B)) continue;
     const long long c = (long long)w.y + threadIdx.x;
+    const double gm1 = a.members ? a.members[B.member].gm1 : p.gm1;
+    if (a.init) {  // dt estimate of the interior
+      unsigned long long cand = ~0ULL;
+      int i, j, k;
+      if (c < B.ncell && is_interior(p, B, c, i, j, k)) {
+        double u[NHYDRO], wv[NHYDRO], g_c, g_e;
+#pragma unroll
+        for (int n = 0; n < NHYDRO; ++n) u[n] = B.u0[n * B.ncell + c];
+        cons_to_prim_cell(u, wv, g_c, g_e, gm1, p.dfloor, p.pfloor);
+        cand = dt_bits(dt_candidate(wv, u[IEN], B.dx, p.ndim, gm1));
+      }
+      if (a.members) member_min(a, B.member, cand);
+      else dtmin = cand < dtmin ? cand : dtmin;
+      continue;
+    }
     if (c >= B.ncell) continue;
     const long long nc = B.ncell;
     double u[NHYDRO], wv[NHYDRO], g_c, g_e;
 #pragma unroll
     for (int n = 0; n < NHYDRO; ++n) u[n] = B.u0[n * nc + c];
     const double ud0 = u[IDN], ue0 = u[IEN];
-    const bool fl = cons_to_prim_cell(u, wv, g_c, g_e, p.gm1, p.dfloor, p.pfloor);
+    const bool fl = cons_to_prim_cell(u, wv, g_c, g_e, gm1, p.dfloor, p.pfloor);
     int i, j, k;
     const bool inner = is_interior(p, B, c, i, j, k);
-    if (a.init) {
-      if (inner) {
-        const unsigned long long bb = dt_bits(dt_candidate(wv, u[IEN], B.dx, p.ndim, p.gm1));
-        dtmin = bb < dtmin ? bb : dtmin;
-      }
-      continue;
-    }
     if (__double_as_longlong(u[IDN]) != __double_as_longlong(ud0)) B.u0[IDN * nc + c] = u[IDN];
     if (__double_as_longlong(u[IEN]) != __double_as_longlong(ue0)) B.u0[IEN * nc + c] = u[IEN];
 #pragma unroll
@@ -567,6 +610,7 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_stage(StageArgs a) {
     for (int it = sched.first(ctr + 2 + pi, nit); it < nit; it = sched.next(ctr + 2 + pi, nit, it)) {
       const int2 w = a.line_items[dir - 1][it];
       const StepBlock &B = a.blocks[w.x];
+      if (!active_of(a, B)) continue;
       const int ntrans = dir == 1 ? B.nx[1] * B.nx[2] : dir == 2 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1];
       const int nl = min(T, ntrans - w.y);
 #if APH_EXACT
@@ -583,7 +627,7 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_stage(StageArgs a) {
     }
     if (!last_pass && !grid_barrier(a.ctl, a.timeout_ns)) return;
   }
-  if (p.amr) {
+  if (a.cf) {
     if (!grid_barrier(a.ctl, a.timeout_ns)) return;
     amr_correct(a, sched, ctr + 6);
     if (!grid_barrier(a.ctl, a.timeout_ns)) return;

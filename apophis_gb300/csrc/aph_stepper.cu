@@ -69,6 +69,59 @@ __global__ void k_dt_policy(StepCtl *c, double cfl) {
   c->bar_count = 0;
 }
 
+// Ensembles: the same policy per member (one CTA over all members), and a summary in the
+// pack's control block: the earliest member time, the largest next dt, the largest cycle
+// count.  initial: dt_0 from the initial estimate.
+__global__ void k_members_policy(StepCtl *c, MemberCtl *m, int n, double cfl, int initial) {
+  __shared__ double s_time[256], s_dt[256];
+  __shared__ int s_cyc[256];
+  double tmin = DBL_MAX, dmax = 0.0;
+  int cyc = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    MemberCtl &x = m[i];
+    double next;
+    if (initial) {
+      next = c->dt_fixed > 0.0 ? c->dt_fixed : min_to_dt(x.min_bits, cfl);
+    } else {
+      const double used = x.active ? x.dt : 0.0;
+      if (used > 0.0) {
+        x.time += used;
+        x.ncycle += 1;
+      }
+      if (c->dt_fixed > 0.0) {
+        next = c->dt_fixed;
+      } else {
+        const double est = min_to_dt(x.min_bits, cfl);
+        const double two = 2.0 * used;
+        next = (est < two) ? est : two;
+      }
+    }
+    if (c->dt_fixed <= 0.0 && x.time < x.tlim && (x.tlim - x.time) < next) next = x.tlim - x.time;
+    x.active = x.time < x.tlim && next > 0.0;
+    x.dt = x.active ? next : 0.0;
+    x.min_bits = ~0ULL;
+    tmin = x.time < tmin ? x.time : tmin;
+    dmax = x.dt > dmax ? x.dt : dmax;
+    cyc = x.ncycle > cyc ? x.ncycle : cyc;
+  }
+  s_time[threadIdx.x] = tmin;
+  s_dt[threadIdx.x] = dmax;
+  s_cyc[threadIdx.x] = cyc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < blockDim.x; ++i) {
+      tmin = s_time[i] < tmin ? s_time[i] : tmin;
+      dmax = s_dt[i] > dmax ? s_dt[i] : dmax;
+      cyc = s_cyc[i] > cyc ? s_cyc[i] : cyc;
+    }
+    c->time = tmin;
+    c->dt = dmax;
+    c->ncycle = cyc;
+    c->min_bits = ~0ULL;
+    c->bar_count = 0;
+  }
+}
+
 struct Stage {
   double gam0, gam1, beta;
 };
@@ -116,6 +169,8 @@ struct aph_stepper_s {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t cap = nullptr;
   std::vector<std::vector<double *>> u0_ptrs;
+  MemberCtl *d_members = nullptr;  // ensembles
+  int nmembers = 0;
 };
 
 namespace {
@@ -233,7 +288,20 @@ StageArgs stage_args(aph_stepper s, int stage_idx, const Stage &st, bool last, b
   a.fix_items = s->d_fix_items;
   a.nfix_items = s->nfix_items;
   a.bflux_stride = s->bflux_stride;
+  a.cf = s->nfix_items > 0;
+  a.members = s->d_members;
   return a;
+}
+
+// End-of-step (or initial) dt policy.
+cudaError_t enqueue_policy(aph_stepper s, bool initial, cudaStream_t st) {
+  if (s->d_members)
+    k_members_policy<<<1, 256, 0, st>>>(s->d_ctl, s->d_members, s->nmembers, s->dev.cfl, initial);
+  else if (initial)
+    k_dt_initial<<<1, 1, 0, st>>>(s->d_ctl, s->dev.cfl);
+  else
+    k_dt_policy<<<1, 1, 0, st>>>(s->d_ctl, s->dev.cfl);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_one(aph_stepper s, const StageArgs &a, int recon, cudaStream_t st) {
@@ -257,8 +325,7 @@ cudaError_t enqueue_step(aph_stepper s, cudaStream_t st) {
     cudaError_t e = launch_one(s, a, recon, st);
     if (e != cudaSuccess) return e;
   }
-  k_dt_policy<<<1, 1, 0, st>>>(s->d_ctl, s->dev.cfl);
-  return cudaGetLastError();
+  return enqueue_policy(s, false, st);
 }
 
 aph_status build_graph(aph_stepper s) {
@@ -297,10 +364,7 @@ aph_status build_graph(aph_stepper s) {
 aph_status initial_dt(aph_stepper s, cudaStream_t st) {
   StageArgs a = stage_args(s, 0, Stage{0, 1, 1}, false, true);
   cudaError_t e = launch_one(s, a, s->params.recon, st);
-  if (e == cudaSuccess) {
-    k_dt_initial<<<1, 1, 0, st>>>(s->d_ctl, s->dev.cfl);
-    e = cudaGetLastError();
-  }
+  if (e == cudaSuccess) e = enqueue_policy(s, true, st);
   return e == cudaSuccess ? APH_OK : cuda_fail(e, "initial dt");
 }
 
@@ -326,6 +390,7 @@ void free_all(aph_stepper s) {
   for (int d = 0; d < 3; ++d) cudaFree(s->d_line_items[d]);
   cudaFree(s->d_fix_items);
   cudaFree(s->d_bflux);
+  cudaFree(s->d_members);
 }
 
 }  // namespace
@@ -362,6 +427,46 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
         return fail(APH_ERR_INVALID, "boundary condition %d not recognized", desc->bc[f]);
   } else if ((long long)desc->nb[0] * desc->nb[1] * desc->nb[2] != desc->nblocks) {
     return fail(APH_ERR_INVALID, "nb product != nblocks");
+  }
+  const aph_ensemble *ens = desc->ensemble;
+  std::vector<MemberCtl> members;
+  if (ens) {
+    if (!amr) return fail(APH_ERR_INVALID, "an ensemble needs face tables (desc.amr)");
+    if (ens->nmembers < 1 || !ens->member || !ens->gm1)
+      return fail(APH_ERR_INVALID, "ensemble: nmembers, member and gm1 are required");
+    for (int b = 0; b < desc->nblocks; ++b) {
+      const int m = ens->member[b];
+      if (m < 0 || m >= ens->nmembers) return fail(APH_ERR_INVALID, "block %d: member %d out of range", b, m);
+      for (int f = 0; f < 4; ++f) {
+        if (desc->amr[b].face_kind[f] == APH_FACE_FINER || desc->amr[b].face_kind[f] == APH_FACE_COARSER)
+          return fail(APH_ERR_UNSUPPORTED, "ensemble members are unrefined meshes");
+        for (int n = 0; n < desc->amr[b].face_count[f]; ++n)
+          if (ens->member[desc->amr[b].face_nbr[f][n]] != m)
+            return fail(APH_ERR_INVALID, "block %d face %d: neighbour in another member", b, f);
+      }
+    }
+    members.resize(ens->nmembers);
+    for (int m = 0; m < ens->nmembers; ++m) {
+      const double gm1 = ens->gm1[m];
+      if (!(gm1 > 0.0) || !std::isfinite(gm1)) return fail(APH_ERR_INVALID, "member %d: gm1 must be > 0", m);
+      PackDev g;
+      std::memset(&g, 0, sizeof(g));
+      g.gm1 = gm1;
+      fill_gas_consts(g);
+      MemberCtl &x = members[m];
+      std::memset(&x, 0, sizeof(x));
+      x.gm1 = g.gm1;
+      x.igm1 = g.igm1;
+      x.gamma = g.gamma;
+      x.c2g = g.c2g;
+      x.one_igm1 = g.one_igm1;
+      x.hlle_k = g.hlle_k;
+      x.hllc_k = g.hllc_k;
+      const double t = ens->tlim && ens->tlim[m] > 0 ? ens->tlim[m] : desc->tlim;
+      x.tlim = t > 0 ? t : DBL_MAX;
+      x.min_bits = ~0ULL;
+      x.active = 1;
+    }
   }
   aph_stepper s = new aph_stepper_s();
   s->params = desc->params;
@@ -425,6 +530,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
     B.nk = ndim >= 3 ? a.nx[2] + 2 * p.ng : 1;
     B.ncell = (long long)B.ni * B.nj * B.nk;
     B.nint = (long long)a.nx[0] * a.nx[1] * a.nx[2];
+    if (ens) B.member = ens->member[b];
     if (amr) {
       static_assert(sizeof(AmrFaces) == sizeof(aph_amr_block), "face table layout");
       std::memcpy(&B.amr, &desc->amr[b], sizeof(AmrFaces));
@@ -459,6 +565,12 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   ck(cudaMalloc(&s->d_flags, sizeof(int) * p.nblocks));
   ck(cudaMalloc(&s->d_ctl, sizeof(StepCtl)));
   ck(cudaMalloc(&s->d_blocks, sizeof(StepBlock) * p.nblocks));
+  if (ens) {
+    s->nmembers = ens->nmembers;
+    ck(cudaMalloc(&s->d_members, sizeof(MemberCtl) * members.size()));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(s->d_members, members.data(), sizeof(MemberCtl) * members.size(), cudaMemcpyHostToDevice);
+  }
   if (amr) {
     s->bflux_stride = 5 * std::max(p.max_nx[0], p.max_nx[1]);
     ck(cudaMalloc(&s->d_bflux, sizeof(double) * 4 * s->bflux_stride * p.nblocks));
@@ -566,6 +678,25 @@ aph_status aph_stepper_status(aph_stepper s, double *time, double *dt, int *ncyc
   return st;
 }
 
+aph_status aph_stepper_member_status(aph_stepper s, double *time, double *dt, int *ncycle,
+                                     void *stream) {
+  clear_error();
+  if (!s) return fail(APH_ERR_INVALID, "stepper is NULL");
+  if (!s->d_members) return fail(APH_ERR_INVALID, "the stepper has no ensemble");
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  std::vector<MemberCtl> m(s->nmembers);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m.data(), s->d_members, sizeof(MemberCtl) * m.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "member status");
+  for (int i = 0; i < s->nmembers; ++i) {
+    if (time) time[i] = m[i].time;
+    if (dt) dt[i] = m[i].dt;
+    if (ncycle) ncycle[i] = m[i].ncycle;
+  }
+  StepCtl c;
+  return read_ctl(s, &c);
+}
+
 aph_status aph_stepper_get_config(aph_stepper s, aph_stepper_config *cfg) {
   clear_error();
   if (!s || !cfg) return fail(APH_ERR_INVALID, "NULL argument");
@@ -628,10 +759,7 @@ aph_status aph_stepper_profile(aph_stepper s, int nsteps, double *stage_ms, void
                                                      s->smem, s->cooperative, st);
       if (e == cudaSuccess) e = cudaEventRecord(ev[2 * (k * ns + i) + 1], st);
     }
-    if (e == cudaSuccess) {
-      k_dt_policy<<<1, 1, 0, st>>>(s->d_ctl, s->dev.cfl);
-      e = cudaGetLastError();
-    }
+    if (e == cudaSuccess) e = enqueue_policy(s, false, st);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   for (int i = 0; i < ns; ++i) stage_ms[i] = 0.0;
@@ -664,6 +792,10 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
   }
   StepCtl ctl_saved;
   e = cudaMemcpy(&ctl_saved, s->d_ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost);
+  std::vector<MemberCtl> members_saved(s->nmembers);
+  if (e == cudaSuccess && s->nmembers)
+    e = cudaMemcpy(members_saved.data(), s->d_members, sizeof(MemberCtl) * s->nmembers,
+                   cudaMemcpyDeviceToHost);
   long long off = 0;
   for (const StepBlock &B : s->hblocks) {
     if (e == cudaSuccess) e = cudaMemcpy(s->d_backup + 5 * off, B.u0, nb5 * B.ncell, cudaMemcpyDeviceToDevice);
@@ -677,6 +809,9 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
       o += B.ncell;
     }
     cudaMemcpy(s->d_ctl, &ctl_saved, sizeof(StepCtl), cudaMemcpyHostToDevice);
+    if (s->nmembers)
+      cudaMemcpy(s->d_members, members_saved.data(), sizeof(MemberCtl) * s->nmembers,
+                 cudaMemcpyHostToDevice);
   };
   // candidate set
   std::vector<aph_stepper_config> cands;

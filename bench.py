@@ -20,6 +20,11 @@ amr     the uneven refined pack (2D Rayleigh-Taylor, 256 x 768 base grid, two st
         1440 meshblocks of 32^2 and 16^2, PPM+HLLC, RK2, gravity): the batched stepper
         against the plain per-pack and per-meshblock launch paths (the latter host-driven,
         and replayed from a CUDA graph as its best case).
+ensemble the batched blast ensemble (64 independent 2D blast problems, grids from
+        {128..512}^2 in 64^2 blocks, gamma ~ U[1.4, 5/3], PPM+HLLC, RK2) run to t = 0.1 in one
+        stepper (one persistent launch per stage over all 1814 blocks, each member with its own
+        gamma, CFL dt and clock; finished members are skipped); zone-updates/s counts every
+        member's own steps.
 adjoint the adjoint/forward time ratio on the differentiable rollout (2D KH 512^2 as 64
         blocks of 64^2, PLM+HLLE, RK2, checkpoint every 20 steps): reverse sweep (with
         recomputation) per step over the batched forward step.
@@ -225,6 +230,33 @@ def amr_leg(args, warmup):
     return out
 
 
+def ensemble_leg(args):
+    """The batched blast ensemble to t = 0.1 (rank 0)."""
+    import torch
+    from apophis_gb300 import ensemble
+    ens, flat = ensemble.blast_ensemble()
+    st = ensemble.EnsembleStepper(ens, flat, exact=False)
+    tune = None if args.no_tune else st.autotune(trial_steps=2)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    a, b = ev(), ev()
+    torch.cuda.synchronize()
+    a.record()
+    launched = st.run_to_end(chunk=16)
+    b.record()
+    torch.cuda.synchronize()
+    sec = a.elapsed_time(b) / 1e3
+    ms = st.member_status()
+    st.close()
+    zu = sum(c.zones() * k for c, k in zip(ens.members, ms["ncycle"]))
+    return {"workload": "64 blast2d members (%d blocks of 64^2, %d zones), PPM+HLLC, RK2, "
+                        "CFL 0.3, to t = 0.1" % (ens.nblocks, ens.zones()),
+            "value": zu / sec, "unit": UNIT, "seconds": sec, "zone_updates": zu,
+            "member_steps_min_max": [min(ms["ncycle"]), max(ms["ncycle"])],
+            "steps_launched": launched, "launches_per_step": 3,
+            "launch": tune["config"] if tune else None,
+            "end_time_min_max": [min(ms["time"]), max(ms["time"])]}
+
+
 def adjoint_leg(nsteps=40):
     """Adjoint/forward time ratio on the differentiable rollout (rank 0)."""
     import torch
@@ -295,6 +327,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the per-meshblock path")
     ap.add_argument("--no-amr", action="store_true", help="skip the refined-pack leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint ratio leg")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the blast-ensemble leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -415,6 +448,8 @@ def main():
     if rank == 0 and not args.no_amr:
         line["amr"] = amr_leg(args, args.warmup)
         line["gpu_launches_amr_batched_step"] = 3
+    if rank == 0 and not args.no_ensemble:
+        line["ensemble"] = ensemble_leg(args)
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = adjoint_leg()
     if rank == 0 and not args.no_cpu:

@@ -186,6 +186,18 @@ aph_status aph_hydro_fill_ghosts(aph_pack pack, void *stream);
  * between steps holds the update's raw values. */
 typedef struct aph_stepper_s *aph_stepper;
 
+/* A batch of independent problems (an ensemble) stepped together in one pack: block b belongs
+ * to member member[b]; each member has its own adiabatic index (gm1) and advances with its
+ * own CFL dt and clock to its own end time.  Members must not neighbour one another in the
+ * face tables (aph_stepper_desc.amr, required: each member is its own mesh, e.g. a periodic
+ * box).  No counterpart in the reference, which runs one problem per executable. */
+typedef struct aph_ensemble {
+  int nmembers;
+  const int *member;   /* per block, 0..nmembers-1 */
+  const double *gm1;   /* per member: gamma - 1 (> 0) */
+  const double *tlim;  /* per member: end time; NULL or <= 0: the desc's tlim */
+} aph_ensemble;
+
 typedef struct aph_stepper_desc {
   aph_hydro_params params;   /* nvar must be 5 */
   int integrator;            /* APH_INTEGRATOR_* (parthenon/time/integrator) */
@@ -198,6 +210,7 @@ typedef struct aph_stepper_desc {
   double tlim;               /* parthenon/time/tlim; <= 0: none */
   double fixed_dt;           /* > 0: every step uses this dt instead of the CFL policy */
   const aph_amr_block *amr;  /* NULL: uniform block grid (nb); else the refined 2D mesh */
+  const aph_ensemble *ensemble;  /* NULL: one problem; else the batch (needs amr face tables) */
 } aph_stepper_desc;
 
 /* Launch configuration, chosen by aph_stepper_autotune or set by hand. */
@@ -220,6 +233,11 @@ aph_status aph_stepper_step(aph_stepper stepper, int nsteps, void *stream);
  * returns APH_ERR_TIMEOUT if a stage's grid barrier gave up. */
 aph_status aph_stepper_status(aph_stepper stepper, double *time, double *dt, int *ncycle,
                               void *stream);
+/* Ensembles: per member (arrays of nmembers) time, the dt of its next step (0 once it has
+ * reached its end time) and cycle count.  aph_stepper_status then reports the earliest
+ * member time, the largest next dt and the largest cycle count. */
+aph_status aph_stepper_member_status(aph_stepper stepper, double *time, double *dt, int *ncycle,
+                                     void *stream);
 aph_status aph_stepper_get_config(aph_stepper stepper, aph_stepper_config *cfg);
 aph_status aph_stepper_set_config(aph_stepper stepper, const aph_stepper_config *cfg);
 /* Advance nsteps steps without the graph, timing each stage launch with CUDA events on

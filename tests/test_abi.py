@@ -91,3 +91,55 @@ def test_null_pack_calls_fail_cleanly():
     d = ctypes.c_double()
     assert lib.aph_hydro_estimate_timestep(None, ctypes.byref(d), None) == 1
     assert lib.aph_pack_destroy(None) == 0
+
+
+def test_stepper_rejects_bad_ensembles():
+    """Validation runs before any device work, so it is checked without a GPU."""
+    import ctypes
+    from apophis_gb300 import ensemble, problems
+    lib = _capi.load()
+    cfgs = [problems.blast2d(n=32, block=16)[0], problems.blast2d(n=32, block=16)[0]]
+    ens = ensemble.Ensemble(cfgs, [0.1, 0.1])
+    blks = ens.blocks()
+    nb = ens.nblocks
+    blocks = (_capi.aph_block * nb)()
+    for b, B in enumerate(blks):
+        blocks[b].cons = 4096 * (b + 1)  # never dereferenced: validation fails first
+        blocks[b].nx[:] = [B.nx[0], B.nx[1], 1]
+        blocks[b].dx[:] = [B.dx[0], B.dx[1], 1.0]
+
+    def make(edit_table=None, member=None, gm1=None):
+        table = (_capi.aph_amr_block * nb)()
+        for b, B in enumerate(blks):
+            t = table[b]
+            t.level = B.level
+            t.origin[0], t.origin[1] = B.origin
+            for f in range(4):
+                t.face_kind[f] = B.face_kind[f]
+                t.face_count[f] = len(B.face_nbr[f])
+                for k, x in enumerate(B.face_nbr[f]):
+                    t.face_nbr[f][k] = x
+        if edit_table:
+            edit_table(table)
+        mem = (ctypes.c_int * nb)(*(member or ens.member_of))
+        g = (ctypes.c_double * 2)(*(gm1 or [0.4, 0.5]))
+        e = _capi.aph_ensemble(2, mem, g, None)
+        desc = _capi.aph_stepper_desc()
+        desc.params = _capi.aph_hydro_params(2, 2, 5, 3, 3, 0.4, 1e-10, 1e-10, 0.3, 0)
+        desc.integrator = 2
+        desc.nblocks = nb
+        desc.blocks = ctypes.cast(blocks, ctypes.POINTER(_capi.aph_block))
+        desc.nb[:] = [nb, 1, 1]
+        desc.bc[:] = [0, 0, 0, 0, 0, 0]
+        desc.amr = ctypes.cast(table, ctypes.POINTER(_capi.aph_amr_block))
+        desc.ensemble = ctypes.pointer(e)
+        h = ctypes.c_void_p()
+        return lib.aph_stepper_create(ctypes.byref(desc), ctypes.byref(h)), (table, mem, g, e)
+
+    def cross(t):  # block 0 of member 0 names block 4 (member 1) as its x- neighbour
+        t[0].face_nbr[0][0] = 4
+
+    for kw in (dict(edit_table=cross), dict(member=[0, 0, 0, 0, 1, 1, 1, 5]),
+               dict(gm1=[0.4, -1.0])):
+        st, _keep = make(**kw)
+        assert st == 1, (kw, st, _capi.load().aph_last_error())  # APH_ERR_INVALID
