@@ -1,8 +1,9 @@
 """Adjoint of the hydro step (aph_adjoint_* in include/aph_hydro.h).
 
 ``Adjoint`` runs fixed-dt rollouts with step checkpointing and their reverse sweeps on
-device tensors in pack layout (nblocks, 5, nk, nj, ni).  The torch.autograd wrapper lives
-in the tests only.
+device tensors in pack layout (nblocks, 5, nk, nj, ni); ``EnsembleAdjoint`` does the same
+for an ensemble (every member's reverse sweep in the same launches, a dt per member and
+step).  The torch.autograd wrapper lives in the tests only.
 """
 import ctypes
 
@@ -74,7 +75,58 @@ class Adjoint:
                    _ptr(out), stream_handle())
         return out
 
+    def forward_members(self, u0, dts, checkpoint_every=20):
+        """dts: nsteps rows of one dt per member."""
+        rows = [[float(x) for x in r] for r in dts]
+        flat = [x for r in rows for x in r]
+        arr = (ctypes.c_double * len(flat))(*flat)
+        out = self.empty()
+        _capi.call("aph_adjoint_forward_members", self.h, _ptr(u0), len(rows), arr,
+                   int(checkpoint_every), _ptr(out), stream_handle())
+        return out
+
     def backward(self, lam_final):
         out = self.empty()
         _capi.call("aph_adjoint_backward", self.h, _ptr(lam_final), _ptr(out), stream_handle())
         return out
+
+
+class EnsembleAdjoint(Adjoint):
+    """Adjoint of an ensemble's step (apophis_gb300.ensemble.Ensemble): the state is the flat
+    pack of all members (blocks of equal size); members keep their own gamma and dt."""
+
+    def __init__(self, ens):
+        from .ensemble import EnsembleStepper
+        require_cuda()
+        _capi.load()
+        self.ens = ens
+        c0 = ens.members[0]
+        nb = ens.nblocks
+        blks = ens.blocks()
+        for B in blks:
+            if B.nx != blks[0].nx:
+                raise ValueError("the adjoint needs ensemble blocks of equal size")
+        blocks = (_capi.aph_block * nb)()
+        for b, B in enumerate(blks):
+            blocks[b].cons = 1  # unused by the adjoint, must be non-null
+            blocks[b].nx[:] = [B.nx[0], B.nx[1], 1]
+            blocks[b].dx[:] = [B.dx[0], B.dx[1], 1.0]
+        table = EnsembleStepper.face_table(blks)
+        self._member = (ctypes.c_int * nb)(*ens.member_of)
+        self._gm1 = (ctypes.c_double * ens.nmembers)(*[c.gm1 for c in ens.members])
+        self._ens = _capi.aph_ensemble(ens.nmembers, self._member, self._gm1, None)
+        self._blocks, self._table = blocks, table
+        desc = _capi.aph_stepper_desc()
+        desc.params = _capi.aph_hydro_params(2, c0.ng, 5, _capi.RECON[c0.recon],
+                                             _capi.RSOLVER[c0.rsolver], c0.gm1, c0.dfloor,
+                                             c0.pfloor, c0.cfl, 0)
+        desc.integrator = _capi.INTEGRATOR[c0.integrator]
+        desc.nblocks = nb
+        desc.blocks = ctypes.cast(blocks, ctypes.POINTER(_capi.aph_block))
+        desc.nb[:] = [nb, 1, 1]
+        desc.bc[:] = [_capi.BC[c0.bc[d][s]] for d in range(2) for s in range(2)] + [0, 0]
+        desc.amr = ctypes.cast(table, ctypes.POINTER(_capi.aph_amr_block))
+        desc.ensemble = ctypes.pointer(self._ens)
+        self.h = ctypes.c_void_p()
+        _capi.call("aph_adjoint_create", ctypes.byref(desc), ctypes.byref(self.h))
+        self.shape = (5 * ens.total_cells,)

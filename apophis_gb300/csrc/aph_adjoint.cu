@@ -5,13 +5,15 @@
 // backwards:
 //     a_{S+1} = lambda^{n+1};   for s = S..1:  acc += gam1_s a_{s+1},
 //     a_s = gam0_s a_{s+1} + R'(u_s)^T (beta_s dt a_{s+1});      lambda^n = a_1 + acc.
-// R'(u)^T mu is one pass per direction (recompute the face states, HLLE/HLLC vjp, PLM/DC
+// R'(u)^T mu is one pass per direction (recompute the face states, HLLE/HLLC vjp, PPM/PLM/DC
 // vjp, gathered per cell without atomics), then the ConsToPrim vjp per cell, then the ghost
-// map transposed (each interior cell gathers the ghost copies made of it).  The forward
-// used for the tape and the recomputation is the per-pack fast path.  Rollouts store a
-// checkpoint every K steps and recompute each segment during the backward sweep, so the
-// memory is (N/K + K) states.  Floors are taken as inactive (the derivative of a floored
-// cell is undefined); a forward that fires a floor is reported as APH_ERR_STATE.
+// map transposed (each interior cell gathers the ghost copies made of it).  The forward is the
+// batched stage kernel of an internal stepper over the adjoint's state, so the adjoint
+// linearises exactly the step the batched path takes, ensembles (per-member gamma and dt)
+// included.  Rollouts store a checkpoint every K steps; the reverse sweep recomputes each
+// segment once, keeping the primitives of every stage input.  Floors are taken as inactive
+// (the derivative of a floored cell is undefined); a forward that fires one is reported as
+// APH_ERR_STATE.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -24,15 +26,29 @@ using namespace aph;
 
 namespace {
 
+struct AdjBlock {
+  double dx[3];
+  int member;
+  int loc[3];       // position in a uniform block grid
+  AmrFaces faces;   // face tables (same-level and boundary faces)
+};
+
+struct AdjMember {
+  GasConsts gc;
+  double ic2g;      // 1 / (C^2 gamma)
+};
+
+// Geometry of the pack (all blocks have the same interior size) and per-block / per-member
+// descriptors on the device.
 struct AdjGeom {
   int nblocks, ndim, ng;
   int nx[3], ni, nj, nk;
   long long ncell;       // per block, entire
   int nb[3];
   int bc[3][2];
-  double dx[3];
-  GasConsts gc;
-  double ic2g;  // 1 / (C^2 gamma)
+  int faces;             // 1: the ghost map comes from face tables
+  const AdjBlock *blk;
+  const AdjMember *mem;
 };
 
 __host__ __device__ __forceinline__ long long blk_off(const AdjGeom &g, int b) {
@@ -56,16 +72,57 @@ __device__ __forceinline__ void adj_line(const AdjGeom &g, int l, long long &bas
   }
 }
 
+// mu-difference scale of a block: beta dt (of its member) * area / volume
+template <int DIR>
+__device__ __forceinline__ double pass_scale(const AdjGeom &g, int b, double beta, const double *dt) {
+  const AdjBlock &B = g.blk[b];
+  const double vol = B.dx[0] * B.dx[1] * B.dx[2];
+  const double area = DIR == 1 ? B.dx[1] * B.dx[2] : DIR == 2 ? B.dx[0] * B.dx[2] : B.dx[0] * B.dx[1];
+  return beta * dt[B.member] * (area / vol);
+}
+
+// Riemann vjp of faces 0..n of nl lines: SL/SR are the face states (slot f / f+1 of width W2),
+// MU the stage adjoint of the interior cells; writes GL/GR (adjoints of the face states).
+template <int DIR, int RS>
+__device__ __forceinline__ void riemann_pass_vjp(const AdjMember &M, int T, int nl, int n, int W2,
+                                                 const double *SL, const double *SR,
+                                                 const double *MU, double scale, double *GL,
+                                                 double *GR) {
+  constexpr int ivx = DIR;
+  constexpr int ivy = IV1 + ((ivx - IV1) + 1) % 3;
+  constexpr int ivz = IV1 + ((ivx - IV1) + 2) % 3;
+  const int perm[5] = {IDN, ivx, ivy, ivz, IEN};
+  for (int it = threadIdx.x; it < nl * (n + 1); it += blockDim.x) {  // faces 0..n
+    const int t = it / (n + 1), f = it % (n + 1);
+    double wl[5], wr[5], gf[5], gwl[5], gwr[5];
+    for (int k = 0; k < 5; ++k) {
+      const int v = perm[k];
+      wl[k] = SL[(v * T + t) * W2 + f];
+      wr[k] = SR[(v * T + t) * W2 + f + 1];
+      const double mhi = f < n ? MU[(v * T + t) * n + f] : 0.0;
+      const double mlo = f > 0 ? MU[(v * T + t) * n + f - 1] : 0.0;
+      gf[k] = scale * (mhi - mlo);
+    }
+    if (RS == RS_HLLE) hlle_vjp(wl, wr, M.gc, M.ic2g, gf, gwl, gwr);
+    else hllc_vjp(wl, wr, M.gc, M.ic2g, gf, gwl, gwr);
+    for (int k = 0; k < 5; ++k) {
+      GL[(perm[k] * T + t) * W2 + f] = gwl[k];
+      GR[(perm[k] * T + t) * W2 + f] = gwr[k];
+    }
+  }
+}
+
+// PLM / donor-cell pass.
 template <int DIR, int RECON, int RS>
 __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim, const double *mu,
-                                                  double *lam_w, double scale, int T) {
+                                                  double *lam_w, double beta, const double *dt, int T) {
   extern __shared__ double sm[];
   constexpr int G = RECON == RECON_PLM ? 2 : 1;
   const int b = blockIdx.y;
   const int n = g.nx[DIR - 1];
   const int ntrans = DIR == 1 ? g.nx[1] * g.nx[2] : DIR == 2 ? g.nx[0] * g.nx[2] : g.nx[0] * g.nx[1];
   const int l0 = blockIdx.x * T;
-  if (l0 >= ntrans) return;
+  if (l0 >= ntrans || dt[g.blk[b].member] == 0.0) return;  // a member that did not move
   const int nl = min(T, ntrans - l0);
   const int NW = n + 2 * G, W2 = n + 2;
   double *W = sm;                             // [5][T][NW]  prim window
@@ -77,7 +134,7 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
   double *CC = GR + 5 * T * W2;               // [3][5][T][W2] recon vjp contributions
   double *RR = CC + 3 * 5 * T * W2;           // [5][T][W2]  PLM reciprocal per cell (0: flat)
   const double *P = prim + blk_off(g, b);
-  const double *M = mu + blk_off(g, b);
+  const double *Mu = mu + blk_off(g, b);
   double *LW = lam_w + blk_off(g, b);
   const long long nc = g.ncell;
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -91,7 +148,7 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
     const int v = it / (nl * n), r = it % (nl * n), t = r / n, c = r % n;
     long long base, s;
     adj_line<DIR>(g, l0 + t, base, s);
-    MU[(v * T + t) * n + c] = M[v * nc + base + (long long)c * s];
+    MU[(v * T + t) * n + c] = Mu[v * nc + base + (long long)c * s];
   }
   __syncthreads();
   auto q = [&](int v, int t, int c) { return W[(v * T + t) * NW + c + G]; };
@@ -104,28 +161,8 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
     SR[(v * T + t) * W2 + c + 1] = qr;
   }
   __syncthreads();
-  constexpr int ivx = DIR;
-  constexpr int ivy = IV1 + ((ivx - IV1) + 1) % 3;
-  constexpr int ivz = IV1 + ((ivx - IV1) + 2) % 3;
-  const int perm[5] = {IDN, ivx, ivy, ivz, IEN};
-  for (int it = tid; it < nl * (n + 1); it += nth) {  // faces 0..n
-    const int t = it / (n + 1), f = it % (n + 1);
-    double wl[5], wr[5], gf[5], gwl[5], gwr[5];
-    for (int k = 0; k < 5; ++k) {
-      const int v = perm[k];
-      wl[k] = SL[(v * T + t) * W2 + f];
-      wr[k] = SR[(v * T + t) * W2 + f + 1];
-      const double mhi = f < n ? MU[(v * T + t) * n + f] : 0.0;
-      const double mlo = f > 0 ? MU[(v * T + t) * n + f - 1] : 0.0;
-      gf[k] = scale * (mhi - mlo);
-    }
-    if (RS == RS_HLLE) hlle_vjp(wl, wr, g.gc, g.ic2g, gf, gwl, gwr);
-    else hllc_vjp(wl, wr, g.gc, g.ic2g, gf, gwl, gwr);
-    for (int k = 0; k < 5; ++k) {
-      GL[(perm[k] * T + t) * W2 + f] = gwl[k];
-      GR[(perm[k] * T + t) * W2 + f] = gwr[k];
-    }
-  }
+  riemann_pass_vjp<DIR, RS>(g.mem[g.blk[b].member], T, nl, n, W2, SL, SR, MU,
+                            pass_scale<DIR>(g, b, beta, dt), GL, GR);
   __syncthreads();
   const size_t cs = (size_t)5 * T * W2;
   for (int it = tid; it < 5 * nl * W2; it += nth) {  // cells -1..n: recon vjp
@@ -160,6 +197,136 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
   }
 }
 
+// PPM pass.  Shared memory: 14 slabs of [5][T][n+6] doubles.
+__host__ __device__ constexpr size_t ppm_pass_slab(int n, int T) { return (size_t)5 * T * (n + 6); }
+
+template <int DIR, int RS>
+__global__ void __launch_bounds__(256) k_adj_pass_ppm(AdjGeom g, const double *prim, const double *mu,
+                                                      double *lam_w, double beta, const double *dt, int T) {
+  extern __shared__ double sm[];
+  constexpr int G = 3;
+  const int b = blockIdx.y;
+  const int n = g.nx[DIR - 1];
+  const int ntrans = DIR == 1 ? g.nx[1] * g.nx[2] : DIR == 2 ? g.nx[0] * g.nx[2] : g.nx[0] * g.nx[1];
+  const int l0 = blockIdx.x * T;
+  if (l0 >= ntrans || dt[g.blk[b].member] == 0.0) return;  // a member that did not move
+  const int nl = min(T, ntrans - l0);
+  const int NW = n + 6, W4 = n + 4, W3 = n + 3, W2 = n + 2;
+  const size_t S = ppm_pass_slab(n, T);
+  double *W = sm;             // cells -3..n+2            (later FQ0)
+  double *MU = sm + 1 * S;    // interior                 (later FQ1)
+  double *D2 = sm + 2 * S;    // cells -2..n+1            (later GL, then FQ2)
+  double *DD = sm + 3 * S;    // cells -2..n+1            (later GR, then FQ3)
+  double *DPH = sm + 4 * S;   // faces -1..n+1
+  double *SL = sm + 5 * S;    // cells -1..n              (later CQ0)
+  double *SR = sm + 6 * S;    //                          (later CQ1)
+  double *RHO = sm + 7 * S;   // cells -1..n
+  double *CQ2 = sm + 8 * S, *CQ3 = sm + 9 * S, *CQ4 = sm + 10 * S;
+  double *GDL = sm + 11 * S, *GDH = sm + 12 * S;  // adjoints of each cell's two face values
+  int *FB = (int *)(sm + 13 * S);                  // face branch, faces -1..n+1
+  int *CB = FB + 5 * T * W3;                       // cell branch, cells -1..n
+  double *GL = D2, *GR = DD;
+  double *const CQ[5] = {SL, SR, CQ2, CQ3, CQ4};
+  double *const FQ[4] = {W, MU, D2, DD};
+  const double *P = prim + blk_off(g, b);
+  const double *Mu = mu + blk_off(g, b);
+  double *LW = lam_w + blk_off(g, b);
+  const long long nc = g.ncell;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int it = tid; it < 5 * nl * NW; it += nth) {
+    const int v = it / (nl * NW), r = it % (nl * NW), t = r / NW, w = r % NW;
+    long long base, s;
+    adj_line<DIR>(g, l0 + t, base, s);
+    W[(v * T + t) * NW + w] = P[v * nc + base + (long long)(w - G) * s];
+  }
+  for (int it = tid; it < 5 * nl * n; it += nth) {
+    const int v = it / (nl * n), r = it % (nl * n), t = r / n, c = r % n;
+    long long base, s;
+    adj_line<DIR>(g, l0 + t, base, s);
+    MU[(v * T + t) * n + c] = Mu[v * nc + base + (long long)c * s];
+  }
+  __syncthreads();
+  auto q = [&](int v, int t, int c) { return W[(v * T + t) * NW + c + G]; };
+  for (int it = tid; it < 5 * nl * W4; it += nth) {  // cells -2..n+1
+    const int v = it / (nl * W4), r = it % (nl * W4), t = r / W4, c = r % W4 - 2;
+    D2[(v * T + t) * W4 + c + 2] = ppm_d2(q(v, t, c - 1), q(v, t, c), q(v, t, c + 1));
+    DD[(v * T + t) * W4 + c + 2] = ppm_dd(q(v, t, c - 1), q(v, t, c), q(v, t, c + 1));
+  }
+  __syncthreads();
+  for (int it = tid; it < 5 * nl * W3; it += nth) {  // faces -1..n+1
+    const int v = it / (nl * W3), r = it % (nl * W3), t = r / W3, f = r % W3 - 1;
+    const size_t o4 = (size_t)(v * T + t) * W4;
+    int code;
+    DPH[(v * T + t) * W3 + f + 1] = ppm_face_code(q(v, t, f - 1), q(v, t, f), DD[o4 + f + 1], DD[o4 + f + 2],
+                                                  D2[o4 + f + 1], D2[o4 + f + 2], code);
+    FB[(v * T + t) * W3 + f + 1] = code;
+  }
+  __syncthreads();
+  for (int it = tid; it < 5 * nl * W2; it += nth) {  // cells -1..n
+    const int v = it / (nl * W2), r = it % (nl * W2), t = r / W2, c = r % W2 - 1;
+    const size_t o4 = (size_t)(v * T + t) * W4, o3 = (size_t)(v * T + t) * W3, o2 = (size_t)(v * T + t) * W2;
+    double ql, qr, rho;
+    int code;
+    ppm_cell_code(q(v, t, c - 2), q(v, t, c - 1), q(v, t, c), q(v, t, c + 1), q(v, t, c + 2), D2[o4 + c + 1],
+                  D2[o4 + c + 2], D2[o4 + c + 3], DPH[o3 + c + 1], DPH[o3 + c + 2], ql, qr, code, rho);
+    SL[o2 + c + 1] = ql;
+    SR[o2 + c + 1] = qr;
+    RHO[o2 + c + 1] = rho;
+    CB[o2 + c + 1] = code;
+  }
+  __syncthreads();
+  riemann_pass_vjp<DIR, RS>(g.mem[g.blk[b].member], T, nl, n, W2, SL, SR, MU,
+                            pass_scale<DIR>(g, b, beta, dt), GL, GR);
+  __syncthreads();
+  // cells -1..n: limiter vjp (CQ0/CQ1 overwrite SL/SR, dead after the Riemann vjp)
+  for (int it = tid; it < 5 * nl * W2; it += nth) {
+    const int v = it / (nl * W2), r = it % (nl * W2), t = r / W2, c = r % W2 - 1;
+    const size_t o2 = (size_t)(v * T + t) * W2, o3 = (size_t)(v * T + t) * W3;
+    const double gL = c + 1 <= n ? GL[o2 + c + 1] : 0.0;  // adjoint of ql_{c+1}
+    const double gR = c >= 0 ? GR[o2 + c] : 0.0;          // adjoint of qr_c
+    double gq[5], glo, ghi;
+    ppm_cell_vjp(q(v, t, c), DPH[o3 + c + 1], DPH[o3 + c + 2], CB[o2 + c + 1], RHO[o2 + c + 1], gL, gR, gq,
+                 glo, ghi);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) CQ[k][o2 + c + 1] = gq[k];
+    GDL[o2 + c + 1] = glo;
+    GDH[o2 + c + 1] = ghi;
+  }
+  __syncthreads();
+  // faces -1..n+1: face-value vjp (FQ overwrite W, MU, GL, GR, all dead now)
+  for (int it = tid; it < 5 * nl * W3; it += nth) {
+    const int v = it / (nl * W3), r = it % (nl * W3), t = r / W3, f = r % W3 - 1;
+    const size_t o2 = (size_t)(v * T + t) * W2, o3 = (size_t)(v * T + t) * W3;
+    // face f is the high face of cell f-1 and the low face of cell f (cells -1..n)
+    double gd = 0.0;
+    if (f - 1 >= -1) gd += GDH[o2 + f];
+    if (f <= n) gd += GDL[o2 + f + 1];
+    double cf[4];
+    ppm_face_coef(FB[o3 + f + 1], cf);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) FQ[k][o3 + f + 1] = gd * cf[k];
+  }
+  __syncthreads();
+  for (int it = tid; it < 5 * nl * NW; it += nth) {  // cells -3..n+2: gather
+    const int v = it / (nl * NW), r = it % (nl * NW), t = r / NW, c = r % NW - 3;
+    const size_t o2 = (size_t)(v * T + t) * W2, o3 = (size_t)(v * T + t) * W3;
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {  // cell c' = c - (k - 2) in -1..n: its gq[k] is for cell c
+      const int cp = c - (k - 2);
+      if (cp >= -1 && cp <= n) acc += CQ[k][o2 + cp + 1];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {  // face f = c - (k - 2) in -1..n+1: its coefficient k is for cell c
+      const int f = c - (k - 2);
+      if (f >= -1 && f <= n + 1) acc += FQ[k][o3 + f + 1];
+    }
+    long long base, s;
+    adj_line<DIR>(g, l0 + t, base, s);
+    LW[v * nc + base + (long long)c * s] += acc;
+  }
+}
+
 // ---- ConsToPrim vjp over the entire domain ----------------------------------------------
 __global__ void k_c2p_vjp(AdjGeom g, const double *w, const double *lam_w, double *lam_u) {
   const int b = blockIdx.y;
@@ -171,7 +338,7 @@ __global__ void k_c2p_vjp(AdjGeom g, const double *w, const double *lam_w, doubl
     ww[v] = w[o + v * nc + c];
     gw[v] = lam_w[o + v * nc + c];
   }
-  cons_to_prim_vjp(ww, gw, g.gc.gm1, gu);
+  cons_to_prim_vjp(ww, gw, g.mem[g.blk[b].member].gc.gm1, gu);
   for (int v = 0; v < 5; ++v) lam_u[o + v * nc + c] = gu[v];
 }
 
@@ -186,7 +353,7 @@ __global__ void k_ghost_vjp(AdjGeom g, const double *lam_u, double *a, double *a
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nint) return;
   const int ii[3] = {idx % g.nx[0], (idx / g.nx[0]) % g.nx[1], idx / (g.nx[0] * g.nx[1])};
-  const int loc[3] = {b % g.nb[0], (b / g.nb[0]) % g.nb[1], b / (g.nb[0] * g.nb[1])};
+  const AdjBlock &B = g.blk[b];
   const long long nc = g.ncell;
   auto cell_of = [&](const int *e) {  // entire-domain index from per-dim entire indices
     return ((long long)e[2] * g.nj + e[1]) * g.ni + e[0];
@@ -200,15 +367,24 @@ __global__ void k_ghost_vjp(AdjGeom g, const double *lam_u, double *a, double *a
     for (int side = 0; side < 2; ++side) {
       const int dist = side == 0 ? ii[d] : g.nx[d] - 1 - ii[d];  // distance from that face
       if (dist >= g.ng) continue;
-      const bool edge = side == 0 ? loc[d] == 0 : loc[d] == g.nb[d] - 1;
-      const int bc = g.bc[d][side];
-      if (!edge || bc == APH_BC_PERIODIC) {
-        // the neighbour across that face holds a ghost copy at depth dist
-        int nl[3] = {loc[0], loc[1], loc[2]};
-        nl[d] += side == 0 ? -1 : 1;
-        if (nl[d] < 0) nl[d] += g.nb[d];
-        if (nl[d] >= g.nb[d]) nl[d] -= g.nb[d];
-        const int nbk = (nl[2] * g.nb[1] + nl[1]) * g.nb[0] + nl[0];
+      // the block across that face (if any) holds a ghost copy of this cell at depth dist
+      int nbk = -1, bc = APH_BC_PERIODIC;
+      if (g.faces) {
+        const int face = 2 * d + side;
+        if (B.faces.kind[face] == FACE_SAME) nbk = B.faces.nbr[face][0];
+        else bc = g.bc[d][side];
+      } else {
+        const bool edge = side == 0 ? B.loc[d] == 0 : B.loc[d] == g.nb[d] - 1;
+        bc = g.bc[d][side];
+        if (!edge || bc == APH_BC_PERIODIC) {
+          int nl[3] = {B.loc[0], B.loc[1], B.loc[2]};
+          nl[d] += side == 0 ? -1 : 1;
+          if (nl[d] < 0) nl[d] += g.nb[d];
+          if (nl[d] >= g.nb[d]) nl[d] -= g.nb[d];
+          nbk = (nl[2] * g.nb[1] + nl[1]) * g.nb[0] + nl[0];
+        }
+      }
+      if (nbk >= 0) {
         int ge[3] = {e[0], e[1], e[2]};
         ge[d] = side == 0 ? g.ng + g.nx[d] + dist : g.ng - 1 - dist;
         const long long gc = cell_of(ge);
@@ -245,9 +421,8 @@ __global__ void k_ghost_vjp(AdjGeom g, const double *lam_u, double *a, double *a
   }
 }
 
-// out = alpha * x + beta * y on interior cells (ghost entries of out set to zero)
-__global__ void k_axpby(AdjGeom g, double alpha, const double *x, double beta, const double *y,
-                        double *out) {
+// out = x on interior cells, zero on ghost cells
+__global__ void k_copy_interior(AdjGeom g, const double *x, double *out) {
   const int b = blockIdx.y;
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.ncell) return;
@@ -257,7 +432,7 @@ __global__ void k_axpby(AdjGeom g, double alpha, const double *x, double beta, c
   if (g.ndim >= 3) in = in && k >= g.ng && k < g.ng + g.nx[2];
   for (int v = 0; v < 5; ++v) {
     const long long o = blk_off(g, b) + v * g.ncell + c;
-    out[o] = in ? alpha * x[o] + (y ? beta * y[o] : 0.0) : 0.0;
+    out[o] = in ? x[o] : 0.0;
   }
 }
 
@@ -281,14 +456,20 @@ struct aph_adjoint_s {
   AdjGeom g;
   aph_hydro_params params;
   int integrator = 0;
+  int nmembers = 1;
   size_t n = 0;  // doubles per pack field
-  double *x = nullptr, *u1 = nullptr, *prim = nullptr, *gamma = nullptr, *flux[3] = {nullptr, nullptr, nullptr};
+  double *x = nullptr;  // the forward stepper's state (pack layout)
   double *lam_w = nullptr, *lam_u = nullptr, *a = nullptr, *acc = nullptr;
-  double *states = nullptr;  // per stage input of the step being differentiated
+  double *states = nullptr;  // stage-input primitives of the step being differentiated
+  AdjBlock *d_blk = nullptr;
+  AdjMember *d_mem = nullptr;
   int *floor_flag = nullptr;
-  aph_pack pack = nullptr;
+  aph_stepper st = nullptr;  // the forward
+  std::vector<aph_block> blocks;
   // rollout
-  std::vector<double> dts;
+  int nsteps = 0;
+  double *d_dts = nullptr;   // [nsteps][nmembers], then one scratch row
+  size_t d_dts_len = 0;
   int ckpt_every = 0;
   double *ckpts = nullptr;
   int nckpt = 0;
@@ -296,77 +477,71 @@ struct aph_adjoint_s {
 
 namespace {
 
-cudaError_t fwd_prepare(aph_adjoint A, cudaStream_t s) {
-  // ghosts + FillDerived of A->x
-  if (aph_hydro_fill_ghosts(A->pack, s) != APH_OK) return cudaErrorUnknown;
-  const PackDev &p = pack_dev(A->pack);
-  return aph_fast::launch_cons_to_prim(p, pack_blocks(A->pack), pack_max_ncell(A->pack),
-                                       A->floor_flag, s);
+aph_status ensure_dts(aph_adjoint A, size_t len) {
+  if (len <= A->d_dts_len) return APH_OK;
+  cudaFree(A->d_dts);
+  A->d_dts = nullptr;
+  A->d_dts_len = 0;
+  cudaError_t e = cudaMalloc(&A->d_dts, len * sizeof(double));
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint dt table");
+  A->d_dts_len = len;
+  return APH_OK;
 }
 
-// One fixed-dt RK step of A->x (interior in, interior + ghosts + prim out).  With keep
-// non-null the primitives of every stage input (entire domain) are saved there, one pack
-// field per stage.
-aph_status fwd_step(aph_adjoint A, double dt, double *keep, cudaStream_t s) {
-  const std::vector<StageC> st = stages_for(A->integrator);
-  cudaError_t e = fwd_prepare(A, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(A->u1, A->x, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-  for (size_t i = 0; i < st.size() && e == cudaSuccess; ++i) {
-    if (keep)
-      e = cudaMemcpyAsync(keep + i * A->n, A->prim, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) break;
-    const int recon = (A->integrator == APH_INTEGRATOR_VL2 && i == 0) ? APH_RECON_DC : A->params.recon;
-    if (aph_hydro_calculate_fluxes(A->pack, recon, A->params.rsolver, s) != APH_OK) return APH_ERR_CUDA;
-    if (aph_hydro_update_with_flux_divergence(A->pack, st[i].gam0, st[i].gam1, st[i].beta * dt, s) != APH_OK)
-      return APH_ERR_CUDA;
-    e = fwd_prepare(A, s);
-  }
+// One step of A->x with the per-member dt dt_dev (device); keep: stage-input primitives.
+aph_status fwd_step(aph_adjoint A, const double *dt_dev, double *keep, cudaStream_t s) {
+  cudaError_t e = stepper_step_dt(A->st, dt_dev, keep, A->floor_flag, s);
   return e == cudaSuccess ? APH_OK : cuda_fail(e, "adjoint forward");
 }
 
 template <int DIR>
-cudaError_t launch_pass(aph_adjoint A, int recon, double scale, const double *prim_in,
-                        cudaStream_t s) {
+cudaError_t launch_pass(aph_adjoint A, int recon, double beta, const double *dt_dev,
+                        const double *prim, cudaStream_t s) {
   const AdjGeom &g = A->g;
   const int n = g.nx[DIR - 1];
-  const int T = std::max(1, 256 / (n + 2));
-  const int G = recon == APH_RECON_PLM ? 2 : 1;
-  const size_t smem = sizeof(double) * (5 * T * (n + 2 * G) + 5 * T * n + 4 * 5 * T * (n + 2) +
-                                        3 * 5 * T * (n + 2) + 5 * T * (n + 2));
+  int T;
+  size_t smem;
+  const void *k = nullptr;
+  const bool hlle = A->params.rsolver == APH_RSOLVER_HLLE;
+  if (recon == APH_RECON_PPM) {
+    const size_t per_line = 14 * ppm_pass_slab(n, 1) * sizeof(double);
+    T = std::max(1, std::min(256 / (n + 6), (int)((96 * 1024) / per_line)));
+    smem = 14 * ppm_pass_slab(n, T) * sizeof(double);
+    k = hlle ? (const void *)k_adj_pass_ppm<DIR, RS_HLLE> : (const void *)k_adj_pass_ppm<DIR, RS_HLLC>;
+  } else {
+    T = std::max(1, 256 / (n + 2));
+    const int G = recon == APH_RECON_PLM ? 2 : 1;
+    smem = sizeof(double) * (5 * T * (n + 2 * G) + 5 * T * n + 4 * 5 * T * (n + 2) +
+                             3 * 5 * T * (n + 2) + 5 * T * (n + 2));
+    if (recon == APH_RECON_PLM)
+      k = hlle ? (const void *)k_adj_pass<DIR, RECON_PLM, RS_HLLE> : (const void *)k_adj_pass<DIR, RECON_PLM, RS_HLLC>;
+    else
+      k = hlle ? (const void *)k_adj_pass<DIR, RECON_DC, RS_HLLE> : (const void *)k_adj_pass<DIR, RECON_DC, RS_HLLC>;
+  }
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
   const int ntrans = DIR == 1 ? g.nx[1] * g.nx[2] : DIR == 2 ? g.nx[0] * g.nx[2] : g.nx[0] * g.nx[1];
   dim3 grid((ntrans + T - 1) / T, g.nblocks);
-  const void *k = nullptr;
-  if (recon == APH_RECON_PLM)
-    k = A->params.rsolver == APH_RSOLVER_HLLE ? (const void *)k_adj_pass<DIR, RECON_PLM, RS_HLLE>
-                                              : (const void *)k_adj_pass<DIR, RECON_PLM, RS_HLLC>;
-  else
-    k = A->params.rsolver == APH_RSOLVER_HLLE ? (const void *)k_adj_pass<DIR, RECON_DC, RS_HLLE>
-                                              : (const void *)k_adj_pass<DIR, RECON_DC, RS_HLLC>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   AdjGeom gg = g;
-  const double *prim = prim_in;
   const double *mu = A->a;
   double *lw = A->lam_w;
   int TT = T;
-  void *args[] = {&gg, &prim, &mu, &lw, &scale, &TT};
+  void *args[] = {&gg, &prim, &mu, &lw, &beta, &dt_dev, &TT};
   return cudaLaunchKernel(k, grid, dim3(256), args, smem, s);
 }
 
 // R'(u)^T (beta dt a) for the stage input whose primitives (entire domain, ghosts included)
 // are prim, combined into a / acc (k_ghost_vjp).
-cudaError_t stage_vjp(aph_adjoint A, int recon, double bdt, const double *prim, double gam0,
-                      double gam1, bool acc_zero, double *lam_n, cudaStream_t s) {
+cudaError_t stage_vjp(aph_adjoint A, int recon, double beta, const double *dt_dev, const double *prim,
+                      double gam0, double gam1, bool acc_zero, double *lam_n, cudaStream_t s) {
   const AdjGeom &g = A->g;
   const unsigned gx = (unsigned)((g.ncell + 255) / 256);
   cudaError_t e = cudaMemsetAsync(A->lam_w, 0, A->n * sizeof(double), s);
-  const double vol = g.dx[0] * g.dx[1] * g.dx[2];
-  const double area[3] = {g.dx[1] * g.dx[2], g.dx[0] * g.dx[2], g.dx[0] * g.dx[1]};
-  for (int d = 1; d <= g.ndim && e == cudaSuccess; ++d) {
-    const double scale = bdt * (area[d - 1] / vol);  // mu = beta dt a
-    e = d == 1 ? launch_pass<1>(A, recon, scale, prim, s)
-               : d == 2 ? launch_pass<2>(A, recon, scale, prim, s) : launch_pass<3>(A, recon, scale, prim, s);
-  }
+  for (int d = 1; d <= g.ndim && e == cudaSuccess; ++d)
+    e = d == 1 ? launch_pass<1>(A, recon, beta, dt_dev, prim, s)
+               : d == 2 ? launch_pass<2>(A, recon, beta, dt_dev, prim, s)
+                        : launch_pass<3>(A, recon, beta, dt_dev, prim, s);
   if (e == cudaSuccess) {
     k_c2p_vjp<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, prim, A->lam_w, A->lam_u);
     e = cudaGetLastError();
@@ -380,48 +555,54 @@ cudaError_t stage_vjp(aph_adjoint A, int recon, double bdt, const double *prim, 
   return e;
 }
 
-// lam_n = (d U^{n+1} / d U^n)^T lam_next for the step whose stage inputs' primitives (as
-// fwd_step keeps them: one pack field per stage) are `kept`, with dt.  lam_n may alias
-// lam_next.
-aph_status step_vjp_kept(aph_adjoint A, const double *kept, double dt, const double *lam_next,
-                         double *lam_n, cudaStream_t s) {
+// lam_n = (d U^{n+1} / d U^n)^T lam_next for the step with per-member dt dt_dev whose
+// stage-input primitives (one pack field per stage) are `kept`.  lam_n may alias lam_next.
+aph_status step_vjp_kept(aph_adjoint A, const double *kept, const double *dt_dev,
+                         const double *lam_next, double *lam_n, cudaStream_t s) {
   const std::vector<StageC> st = stages_for(A->integrator);
   const AdjGeom &g = A->g;
   const unsigned gx = (unsigned)((g.ncell + 255) / 256);
-  k_axpby<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, 1.0, lam_next, 0.0, nullptr, A->a);
+  k_copy_interior<<<dim3(gx, g.nblocks), 256, 0, s>>>(g, lam_next, A->a);
   cudaError_t e = cudaGetLastError();
   const int ns = (int)st.size();
   for (int i = ns - 1; i >= 0 && e == cudaSuccess; --i) {
     const int recon = (A->integrator == APH_INTEGRATOR_VL2 && i == 0) ? APH_RECON_DC : A->params.recon;
-    e = stage_vjp(A, recon, st[i].beta * dt, kept + (size_t)i * A->n, st[i].gam0, st[i].gam1,
+    e = stage_vjp(A, recon, st[i].beta, dt_dev, kept + (size_t)i * A->n, st[i].gam0, st[i].gam1,
                   i == ns - 1, i == 0 ? lam_n : nullptr, s);
   }
   return e == cudaSuccess ? APH_OK : cuda_fail(e, "adjoint step");
 }
 
-// The same from the step's input u_n: recompute the step, keeping its stage inputs.
-aph_status step_vjp(aph_adjoint A, const double *u_n, double dt, const double *lam_next,
-                    double *lam_n, cudaStream_t s) {
-  cudaError_t e = cudaMemcpyAsync(A->x, u_n, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(e, "adjoint step");
-  if (aph_status r = fwd_step(A, dt, A->states, s)) return r;
-  return step_vjp_kept(A, A->states, dt, lam_next, lam_n, s);
-}
-
 void adj_free(aph_adjoint A) {
-  if (A->pack) aph_pack_destroy(A->pack);
-  double *bufs[] = {A->x, A->u1, A->prim, A->gamma, A->flux[0], A->flux[1], A->flux[2], A->lam_w,
-                    A->lam_u, A->a, A->acc, A->states, A->ckpts};
+  if (A->st) aph_stepper_destroy(A->st);
+  A->st = nullptr;
+  double *bufs[] = {A->x, A->lam_w, A->lam_u, A->a, A->acc, A->states, A->ckpts, A->d_dts};
   for (double *p : bufs) cudaFree(p);
+  cudaFree(A->d_blk);
+  cudaFree(A->d_mem);
   cudaFree(A->floor_flag);
 }
 
-aph_status check_floor(aph_adjoint A, cudaStream_t s) {
+aph_status check_state(aph_adjoint A, cudaStream_t s) {
   int f = 0;
   cudaError_t e = cudaMemcpyAsync(&f, A->floor_flag, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint");
+  if (aph_status st = aph_stepper_status(A->st, nullptr, nullptr, nullptr, s)) return st;
   if (f) return fail(APH_ERR_STATE, "a density or pressure floor fired: the step is not differentiable there");
+  return APH_OK;
+}
+
+// the same dt for every member, in the scratch row after the rollout table
+aph_status scalar_dt(aph_adjoint A, double dt, const double **dt_dev, cudaStream_t s) {
+  const size_t row = (size_t)A->nsteps * A->nmembers;
+  if (aph_status st = ensure_dts(A, row + A->nmembers)) return st;
+  std::vector<double> v(A->nmembers, dt);
+  cudaError_t e = cudaMemcpyAsync(A->d_dts + row, v.data(), v.size() * sizeof(double),
+                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // v is a host temporary
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint dt");
+  *dt_dev = A->d_dts + row;
   return APH_OK;
 }
 
@@ -436,17 +617,37 @@ aph_status aph_adjoint_create(const aph_stepper_desc *desc, aph_adjoint *out) {
   if (aph_status st = validate_params(&desc->params)) return st;
   const aph_hydro_params &q = desc->params;
   if (q.nvar != 5) return fail(APH_ERR_UNSUPPORTED, "the adjoint carries no passive scalars");
-  if (q.recon != APH_RECON_PLM && q.recon != APH_RECON_DC)
-    return fail(APH_ERR_UNSUPPORTED, "the adjoint differentiates dc and plm reconstruction");
   if (q.rsolver != APH_RSOLVER_HLLE && q.rsolver != APH_RSOLVER_HLLC)
     return fail(APH_ERR_UNSUPPORTED, "the adjoint differentiates the hlle and hllc solvers");
   if (q.exact) return fail(APH_ERR_UNSUPPORTED, "the adjoint runs on the fast arithmetic");
   if (desc->use_gravity) return fail(APH_ERR_UNSUPPORTED, "the adjoint has no gravity source");
   if (stages_for(desc->integrator).empty()) return fail(APH_ERR_INVALID, "integrator not recognized");
   if (desc->nblocks <= 0 || !desc->blocks) return fail(APH_ERR_INVALID, "no blocks");
+  for (int b = 0; b < desc->nblocks; ++b)
+    for (int d = 0; d < 3; ++d)
+      if (desc->blocks[b].nx[d] != desc->blocks[0].nx[d])
+        return fail(APH_ERR_UNSUPPORTED, "the adjoint's pack layout needs blocks of equal size");
+  if (desc->amr)
+    for (int b = 0; b < desc->nblocks; ++b)
+      for (int f = 0; f < 4; ++f) {
+        const int k = desc->amr[b].face_kind[f];
+        if (k == APH_FACE_COARSER || k == APH_FACE_FINER)
+          return fail(APH_ERR_UNSUPPORTED, "the adjoint has no coarse-fine faces");
+        // the transposed gather relies on reciprocal same-level neighbours
+        if (k == APH_FACE_SAME) {
+          const int nb = desc->amr[b].face_nbr[f][0];
+          if (nb < 0 || nb >= desc->nblocks || desc->amr[nb].face_kind[f ^ 1] != APH_FACE_SAME ||
+              desc->amr[nb].face_nbr[f ^ 1][0] != b)
+            return fail(APH_ERR_INVALID, "block %d face %d: same-level neighbours must be reciprocal", b, f);
+        }
+      }
+  const int nmembers = desc->ensemble ? desc->ensemble->nmembers : 1;
+  if (nmembers < 1 || (desc->ensemble && (!desc->ensemble->member || !desc->ensemble->gm1)))
+    return fail(APH_ERR_INVALID, "ensemble: nmembers, member and gm1 are required");
   aph_adjoint A = new aph_adjoint_s();
   A->params = q;
   A->integrator = desc->integrator;
+  A->nmembers = nmembers;
   AdjGeom &g = A->g;
   std::memset(&g, 0, sizeof(g));
   g.nblocks = desc->nblocks;
@@ -454,57 +655,87 @@ aph_status aph_adjoint_create(const aph_stepper_desc *desc, aph_adjoint *out) {
   g.ng = q.nghost;
   for (int d = 0; d < 3; ++d) {
     g.nx[d] = desc->blocks[0].nx[d];
-    g.dx[d] = desc->blocks[0].dx[d];
     g.nb[d] = desc->nb[d];
     g.bc[d][0] = desc->bc[2 * d];
     g.bc[d][1] = desc->bc[2 * d + 1];
   }
+  g.faces = desc->amr ? 1 : 0;
   g.ni = g.nx[0] + 2 * g.ng;
   g.nj = g.ndim >= 2 ? g.nx[1] + 2 * g.ng : 1;
   g.nk = g.ndim >= 3 ? g.nx[2] + 2 * g.ng : 1;
   g.ncell = (long long)g.ni * g.nj * g.nk;
-  PackDev tmp;
-  std::memset(&tmp, 0, sizeof(tmp));
-  tmp.gm1 = q.gm1;
-  fill_gas_consts(tmp);
-  g.gc = GasConsts{tmp.gm1, tmp.igm1, tmp.gamma, tmp.c2g, tmp.one_igm1, tmp.hlle_k, tmp.hllc_k};
-  g.ic2g = 1.0 / tmp.c2g;
   A->n = (size_t)g.nblocks * 5 * g.ncell;
   const size_t bytes = A->n * sizeof(double);
   const int ns = (int)stages_for(A->integrator).size();
+  // per-block and per-member descriptors
+  std::vector<AdjBlock> hb(g.nblocks);
+  for (int b = 0; b < g.nblocks; ++b) {
+    AdjBlock &B = hb[b];
+    std::memset(&B, 0, sizeof(B));
+    for (int d = 0; d < 3; ++d) B.dx[d] = desc->blocks[b].dx[d];
+    B.member = desc->ensemble ? desc->ensemble->member[b] : 0;
+    if (B.member < 0 || B.member >= nmembers) {
+      delete A;
+      return fail(APH_ERR_INVALID, "block %d: member out of range", b);
+    }
+    if (desc->amr) {
+      std::memcpy(&B.faces, &desc->amr[b], sizeof(AmrFaces));
+    } else {
+      const int n0 = std::max(1, g.nb[0]), n1 = std::max(1, g.nb[1]);
+      B.loc[0] = b % n0;
+      B.loc[1] = (b / n0) % n1;
+      B.loc[2] = b / (n0 * n1);
+    }
+  }
+  std::vector<AdjMember> hm(nmembers);
+  for (int m = 0; m < nmembers; ++m) {
+    PackDev tmp;
+    std::memset(&tmp, 0, sizeof(tmp));
+    tmp.gm1 = desc->ensemble ? desc->ensemble->gm1[m] : q.gm1;
+    if (!(tmp.gm1 > 0.0)) {
+      delete A;
+      return fail(APH_ERR_INVALID, "member %d: gm1 must be > 0", m);
+    }
+    fill_gas_consts(tmp);
+    hm[m].gc = GasConsts{tmp.gm1, tmp.igm1, tmp.gamma, tmp.c2g, tmp.one_igm1, tmp.hlle_k, tmp.hllc_k};
+    hm[m].ic2g = 1.0 / tmp.c2g;
+  }
   cudaError_t e = cudaSuccess;
   auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-  double **bufs[] = {&A->x, &A->u1, &A->prim, &A->lam_w, &A->lam_u, &A->a, &A->acc};
+  double **bufs[] = {&A->x, &A->lam_w, &A->lam_u, &A->a, &A->acc};
   for (double **b : bufs) ck(cudaMalloc(b, bytes));
-  ck(cudaMalloc(&A->gamma, bytes / 5 * 2));
-  for (int d = 0; d < g.ndim; ++d) ck(cudaMalloc(&A->flux[d], bytes));
   ck(cudaMalloc(&A->states, bytes * ns));
   ck(cudaMalloc(&A->floor_flag, sizeof(int)));
+  ck(cudaMalloc(&A->d_blk, sizeof(AdjBlock) * hb.size()));
+  ck(cudaMalloc(&A->d_mem, sizeof(AdjMember) * hm.size()));
+  if (e == cudaSuccess) e = cudaMemcpy(A->d_blk, hb.data(), sizeof(AdjBlock) * hb.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(A->d_mem, hm.data(), sizeof(AdjMember) * hm.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(A->floor_flag, 0, sizeof(int));
-  if (e == cudaSuccess) e = cudaMemset(A->x, 0, bytes);
   if (e != cudaSuccess) {
     adj_free(A);
     delete A;
     return cuda_fail(e, "adjoint allocation");
   }
-  std::vector<aph_block> blocks(g.nblocks);
-  for (int b = 0; b < g.nblocks; ++b) {
-    aph_block &B = blocks[b];
-    std::memset(&B, 0, sizeof(B));
-    const size_t o = (size_t)b * 5 * g.ncell;
-    B.cons = A->x + o;
-    B.u1 = A->u1 + o;
-    B.prim = A->prim + o;
-    B.gamma = A->gamma + (size_t)b * 2 * g.ncell;
-    for (int d = 0; d < g.ndim; ++d) B.flux[d] = A->flux[d] + o;
-    for (int d = 0; d < 3; ++d) {
-      B.nx[d] = g.nx[d];
-      B.dx[d] = g.dx[d];
+  g.blk = A->d_blk;
+  g.mem = A->d_mem;
+  // the forward: a stepper over the adjoint's state (a uniform placeholder state, rho = E = 1,
+  // for its initial dt estimate)
+  A->blocks.assign(desc->blocks, desc->blocks + desc->nblocks);
+  for (int b = 0; b < g.nblocks; ++b) A->blocks[b].cons = A->x + (size_t)b * 5 * g.ncell;
+  {
+    std::vector<double> one(5 * g.ncell, 0.0);
+    for (long long c = 0; c < g.ncell; ++c) {
+      one[c] = 1.0;
+      one[4 * g.ncell + c] = 1.0;
     }
+    for (int b = 0; b < g.nblocks && e == cudaSuccess; ++b)
+      e = cudaMemcpy(A->blocks[b].cons, one.data(), one.size() * sizeof(double), cudaMemcpyHostToDevice);
   }
-  aph_hydro_params pq = q;
-  aph_status st = aph_pack_create(&pq, blocks.data(), g.nblocks, &A->pack);
-  if (st == APH_OK) st = aph_pack_set_topology(A->pack, desc->nb, desc->bc);
+  aph_stepper_desc sd = *desc;
+  sd.blocks = A->blocks.data();
+  sd.fixed_dt = 1.0;
+  sd.tlim = 0.0;
+  aph_status st = e == cudaSuccess ? aph_stepper_create(&sd, &A->st) : cuda_fail(e, "adjoint setup");
   if (st) {
     adj_free(A);
     delete A;
@@ -525,13 +756,15 @@ aph_status aph_adjoint_step(aph_adjoint A, const double *u_n, double dt, double 
   clear_error();
   if (!A || !u_n || !u_next) return fail(APH_ERR_INVALID, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
+  const double *dt_dev = nullptr;
+  if (aph_status st = scalar_dt(A, dt, &dt_dev, s)) return st;
   cudaMemsetAsync(A->floor_flag, 0, sizeof(int), s);
   cudaError_t e = cudaMemcpyAsync(A->x, u_n, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint forward");
-  if (aph_status st = fwd_step(A, dt, nullptr, s)) return st;
+  if (aph_status st = fwd_step(A, dt_dev, nullptr, s)) return st;
   e = cudaMemcpyAsync(u_next, A->x, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint forward");
-  return check_floor(A, s);
+  return check_state(A, s);
 }
 
 aph_status aph_adjoint_step_vjp(aph_adjoint A, const double *u_n, double dt, const double *lam_next,
@@ -539,13 +772,18 @@ aph_status aph_adjoint_step_vjp(aph_adjoint A, const double *u_n, double dt, con
   clear_error();
   if (!A || !u_n || !lam_next || !lam_n) return fail(APH_ERR_INVALID, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
+  const double *dt_dev = nullptr;
+  if (aph_status st = scalar_dt(A, dt, &dt_dev, s)) return st;
   cudaMemsetAsync(A->floor_flag, 0, sizeof(int), s);
-  if (aph_status st = step_vjp(A, u_n, dt, lam_next, lam_n, s)) return st;
-  return check_floor(A, s);
+  cudaError_t e = cudaMemcpyAsync(A->x, u_n, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint step");
+  if (aph_status st = fwd_step(A, dt_dev, A->states, s)) return st;
+  if (aph_status st = step_vjp_kept(A, A->states, dt_dev, lam_next, lam_n, s)) return st;
+  return check_state(A, s);
 }
 
-aph_status aph_adjoint_forward(aph_adjoint A, const double *u0, int nsteps, const double *dts,
-                               int checkpoint_every, double *u_final, void *stream) {
+aph_status aph_adjoint_forward_members(aph_adjoint A, const double *u0, int nsteps, const double *dts,
+                                       int checkpoint_every, double *u_final, void *stream) {
   clear_error();
   if (!A || !u0 || !dts || nsteps < 1 || !u_final) return fail(APH_ERR_INVALID, "bad argument");
   if (checkpoint_every < 1) checkpoint_every = nsteps;
@@ -554,36 +792,54 @@ aph_status aph_adjoint_forward(aph_adjoint A, const double *u0, int nsteps, cons
   if (nck != A->nckpt) {
     cudaFree(A->ckpts);
     A->ckpts = nullptr;
+    A->nckpt = 0;
     cudaError_t e = cudaMalloc(&A->ckpts, (size_t)nck * A->n * sizeof(double));
     if (e != cudaSuccess) return cuda_fail(e, "checkpoint allocation");
     A->nckpt = nck;
   }
-  A->dts.assign(dts, dts + nsteps);
+  const size_t nm = A->nmembers;
+  A->nsteps = 0;
+  if (aph_status st = ensure_dts(A, (size_t)nsteps * nm + nm)) return st;
+  cudaError_t e = cudaMemcpyAsync(A->d_dts, dts, (size_t)nsteps * nm * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // dts is the caller's host array
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint dt table");
+  A->nsteps = nsteps;
   A->ckpt_every = checkpoint_every;
   cudaMemsetAsync(A->floor_flag, 0, sizeof(int), s);
-  cudaError_t e = cudaMemcpyAsync(A->x, u0, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  e = cudaMemcpyAsync(A->x, u0, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   for (int k = 0; k < nsteps && e == cudaSuccess; ++k) {
     if (k % checkpoint_every == 0)
       e = cudaMemcpyAsync(A->ckpts + (size_t)(k / checkpoint_every) * A->n, A->x, A->n * sizeof(double),
                           cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) break;
-    if (aph_status st = fwd_step(A, dts[k], nullptr, s)) return st;
+    if (aph_status st = fwd_step(A, A->d_dts + (size_t)k * nm, nullptr, s)) return st;
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(u_final, A->x, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint rollout");
-  return check_floor(A, s);
+  return check_state(A, s);
+}
+
+aph_status aph_adjoint_forward(aph_adjoint A, const double *u0, int nsteps, const double *dts,
+                               int checkpoint_every, double *u_final, void *stream) {
+  clear_error();
+  if (!A || !dts || nsteps < 1) return fail(APH_ERR_INVALID, "bad argument");
+  std::vector<double> table((size_t)nsteps * A->nmembers);
+  for (int k = 0; k < nsteps; ++k)
+    for (int m = 0; m < A->nmembers; ++m) table[(size_t)k * A->nmembers + m] = dts[k];
+  return aph_adjoint_forward_members(A, u0, nsteps, table.data(), checkpoint_every, u_final, stream);
 }
 
 aph_status aph_adjoint_backward(aph_adjoint A, const double *lam_final, double *lam_initial,
                                 void *stream) {
   clear_error();
   if (!A || !lam_final || !lam_initial) return fail(APH_ERR_INVALID, "NULL argument");
-  if (A->dts.empty()) return fail(APH_ERR_INVALID, "no recorded rollout");
+  if (A->nsteps < 1 || !A->ckpts) return fail(APH_ERR_INVALID, "no recorded rollout");
   cudaStream_t s = (cudaStream_t)stream;
-  const int nsteps = (int)A->dts.size(), K = A->ckpt_every;
+  const int nsteps = A->nsteps, K = A->ckpt_every;
+  const size_t nm = A->nmembers;
   const int ns = (int)stages_for(A->integrator).size();
-  // segment storage: the stage inputs of every step of one segment, recomputed once from the
-  // segment's checkpoint
+  // segment storage: the stage-input primitives of every step of one segment, recomputed
+  // once from the segment's checkpoint
   double *seg = nullptr;
   const size_t per_step = (size_t)ns * A->n;
   cudaError_t e = cudaMalloc(&seg, (size_t)K * per_step * sizeof(double));
@@ -594,15 +850,16 @@ aph_status aph_adjoint_backward(aph_adjoint A, const double *lam_final, double *
     const int k0 = j * K, k1 = std::min(nsteps, k0 + K);
     e = cudaMemcpyAsync(A->x, A->ckpts + (size_t)j * A->n, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
     for (int k = k0; k < k1 && st == APH_OK && e == cudaSuccess; ++k)
-      st = fwd_step(A, A->dts[k], seg + (size_t)(k - k0) * per_step, s);
+      st = fwd_step(A, A->d_dts + (size_t)k * nm, seg + (size_t)(k - k0) * per_step, s);
     for (int k = k1 - 1; k >= k0 && st == APH_OK && e == cudaSuccess; --k)
-      st = step_vjp_kept(A, seg + (size_t)(k - k0) * per_step, A->dts[k], lam_initial, lam_initial, s);
+      st = step_vjp_kept(A, seg + (size_t)(k - k0) * per_step, A->d_dts + (size_t)k * nm, lam_initial,
+                         lam_initial, s);
   }
   if (e == cudaSuccess && st == APH_OK) e = cudaStreamSynchronize(s);
   cudaFree(seg);
   if (st) return st;
   if (e != cudaSuccess) return cuda_fail(e, "adjoint backward");
-  return check_floor(A, s);
+  return check_state(A, s);
 }
 
 }  // extern "C"

@@ -63,6 +63,172 @@ __device__ __forceinline__ void plm_vjp(double q_im1, double q_i, double q_ip1, 
   }
 }
 
+// ---- PPM (ppm_simple.hpp:32-161, in the face/cell split of aph_math.cuh) --------------------
+// The forward is piecewise linear in q except the extremum limiter's ratio rho = qe / d2qf,
+// so the reverse records the branch each face and cell took and applies the transposed
+// linear map of that branch (and the quotient rule for rho).
+constexpr int PF_OPEN = 0, PF_AVG = 1, PF_D2M = 2, PF_D20 = 3, PF_QA = 4;
+
+// ppm_face (fast arithmetic) returning the branch: OPEN (unlimited), or limited with
+// qd = 0 (AVG), C2 d2(f-1) (D2M), C2 d2(f) (D20), or qa (QA).
+__device__ __forceinline__ double ppm_face_code(double qm1, double q0, double ddm1, double dd0,
+                                                double d2m1, double d20, int &code) {
+  const double avg = 0.5 * (qm1 + q0);
+  double dph = fma(ddm1 - dd0, 1.0 / 6.0, avg);
+  const double qa_tmp = dph - qm1;
+  const double qb_tmp = q0 - dph;
+  const double qa = 3.0 * (qm1 + q0 - 2.0 * dph);
+  code = PF_OPEN;
+  if (is_neg(qa_tmp * qb_tmp)) {
+    double qd = 0.0;
+    code = PF_AVG;
+    const bool sa = is_neg(qa);
+    if (sa == is_neg(d2m1) && sa == is_neg(d20)) {
+      const unsigned long long mb = mag(d2m1), mc = mag(d20);
+      const bool pick_c = mc < mb;
+      const unsigned long long mm = mag(PPM_C2 * from_bits(pick_c ? mc : mb)), ma = mag(qa);
+      if (ma < mm) {
+        qd = qa;
+        code = PF_QA;
+      } else {
+        qd = flip_if(from_bits(mm), sa);
+        code = pick_c ? PF_D20 : PF_D2M;
+      }
+    }
+    dph = fma(qd, -1.0 / 6.0, avg);
+  }
+  return dph;
+}
+
+// d dph / d (q[f-2], q[f-1], q[f], q[f+1]) of a face with the given branch (dd and d2 are
+// linear; the QA branch gives back the unlimited value).
+__device__ __forceinline__ void ppm_face_coef(int code, double c[4]) {
+  constexpr double a = 1.0 / 12.0, b = PPM_C2 / 6.0;
+  if (code == PF_AVG) {
+    c[0] = 0.0; c[1] = 0.5; c[2] = 0.5; c[3] = 0.0;
+  } else if (code == PF_D2M) {
+    c[0] = -b; c[1] = 0.5 + 2.0 * b; c[2] = 0.5 - b; c[3] = 0.0;
+  } else if (code == PF_D20) {
+    c[0] = 0.0; c[1] = 0.5 - b; c[2] = 0.5 + 2.0 * b; c[3] = -b;
+  } else {
+    c[0] = -a; c[1] = 7.0 * a; c[2] = 7.0 * a; c[3] = -a;
+  }
+}
+
+// ppm_cell (fast arithmetic) returning its branch: bit 0 extremum; extremum: bits 1-3 the
+// source of qe (0 none, 1..3 C2 d2 of cell i-1, i, i+1, 4 d2qf), bit 4 the ratio applied;
+// monotone: bit 1 qr steepened, bit 2 ql steepened.  rho: the ratio used.
+__device__ __forceinline__ void ppm_cell_code(double q_im2, double q_im1, double q_i, double q_ip1,
+                                              double q_ip2, double d2m1, double d20, double d2p1,
+                                              double dph_lo, double dph_hi, double &ql, double &qr,
+                                              int &code, double &rho) {
+  const double d2qf = 6.0 * (dph_lo + dph_hi - 2.0 * q_i);
+  qr = dph_lo;
+  ql = dph_hi;
+  const double dqf_minus = q_i - qr;
+  const double dqf_plus = ql - q_i;
+  const double qa_tmp = dqf_minus * dqf_plus;
+  const double qb_tmp = (q_ip1 - q_i) * (q_i - q_im1);
+  code = 0;
+  rho = 0.0;
+  if (!is_pos(qa_tmp) || !is_pos(qb_tmp)) {
+    code = 1;
+    double qe = 0.0;
+    int src = 0;
+    const bool sd = is_neg(d2qf);
+    if (sd == is_neg(d2m1) && sd == is_neg(d20) && sd == is_neg(d2p1)) {
+      unsigned long long m = mag(d2m1);
+      int k = 1;
+      const unsigned long long m0 = mag(d20), m1 = mag(d2p1);
+      if (m0 < m) { m = m0; k = 2; }
+      if (m1 < m) { m = m1; k = 3; }
+      const unsigned long long ms = mag(PPM_C2 * from_bits(m)), md = mag(d2qf);
+      if (md < ms) {
+        qe = d2qf;
+        src = 4;
+      } else {
+        qe = flip_if(from_bits(ms), sd);
+        src = k;
+      }
+    }
+    unsigned long long mx = mag(q_im2);
+    const unsigned long long a1 = mag(q_im1), a2 = mag(q_i), a3 = mag(q_ip1), a4 = mag(q_ip2);
+    mx = a1 > mx ? a1 : mx;
+    mx = a2 > mx ? a2 : mx;
+    mx = a3 > mx ? a3 : mx;
+    mx = a4 > mx ? a4 : mx;
+    if (mag(d2qf) > mag(1.0e-12 * from_bits(mx))) rho = qe / d2qf;
+    code |= src << 1;
+    if (le(rho, 1.0 - 1.0e-12)) {
+      qr = fma(-rho, dqf_minus, q_i);
+      ql = fma(rho, dqf_plus, q_i);
+      code |= 16;
+    }
+  } else {
+    if (mag(dqf_minus) >= twice_mag(dqf_plus)) {
+      qr = q_i - 2.0 * dqf_plus;
+      code |= 2;
+    }
+    if (mag(dqf_plus) >= twice_mag(dqf_minus)) {
+      ql = q_i + 2.0 * dqf_minus;
+      code |= 4;
+    }
+  }
+}
+
+// Reverse of ppm_cell_code: gL, gR adjoints of ql_{i+1}, qr_i; out: gq (q_{i-2..i+2}) and the
+// adjoints of the two face values.
+__device__ __forceinline__ void ppm_cell_vjp(double q_i, double dph_lo, double dph_hi, int code,
+                                             double rho, double gL, double gR, double gq[5],
+                                             double &g_lo, double &g_hi) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) gq[k] = 0.0;
+  g_lo = 0.0;
+  g_hi = 0.0;
+  if (code & 1) {
+    if (code & 16) {  // ql = q_i + rho (dph_hi - q_i), qr = q_i - rho (q_i - dph_lo)
+      gq[2] += (gL + gR) * (1.0 - rho);
+      g_hi += gL * rho;
+      g_lo += gR * rho;
+      const int src = (code >> 1) & 7;
+      if (rho != 0.0 && src >= 1 && src <= 3) {  // rho = C2 d2(i + src - 2) / d2qf
+        const double d2qf = 6.0 * (dph_lo + dph_hi - 2.0 * q_i);
+        const double g_rho = gL * (dph_hi - q_i) - gR * (q_i - dph_lo);
+        const double g_qe = g_rho / d2qf;
+        const double g_d2qf = -g_qe * rho;
+        g_lo += 6.0 * g_d2qf;
+        g_hi += 6.0 * g_d2qf;
+        gq[2] -= 12.0 * g_d2qf;
+        // d2 of cell i + src - 2 is q[c-1] + q[c+1] - 2 q[c], c at gq index src
+        const double gd = PPM_C2 * g_qe;
+        if (src == 1) {
+          gq[0] += gd; gq[2] += gd; gq[1] -= 2.0 * gd;
+        } else if (src == 2) {
+          gq[1] += gd; gq[3] += gd; gq[2] -= 2.0 * gd;
+        } else {
+          gq[2] += gd; gq[4] += gd; gq[3] -= 2.0 * gd;
+        }
+      }
+    } else {
+      g_hi += gL;
+      g_lo += gR;
+    }
+  } else {
+    if (code & 2) {  // qr = 3 q_i - 2 dph_hi
+      gq[2] += 3.0 * gR;
+      g_hi -= 2.0 * gR;
+    } else {
+      g_lo += gR;
+    }
+    if (code & 4) {  // ql = 3 q_i - 2 dph_lo
+      gq[2] += 3.0 * gL;
+      g_lo -= 2.0 * gL;
+    } else {
+      g_hi += gL;
+    }
+  }
+}
+
 // ---- sound speed c = sqrt(N/D), N = C^2 gamma p, D = p (1 + 1/gm1) + rho C^2 ------------
 // ip = 1/p; 1/D = c^2 / N = c^2 ip / (C^2 gamma), so no division beyond ip.
 struct SoundSpeed {

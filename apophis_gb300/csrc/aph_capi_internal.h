@@ -22,6 +22,15 @@ const aph_hydro_params &pack_params(aph_pack p);
 const std::vector<BlockDev> &pack_host_blocks(aph_pack p);
 bool pack_has_topology(aph_pack p);
 
+// Adjoint support (aph_stepper.cu).  One RK step of the stepper's state with the per-member
+// dt dt_dev (a device array of nmembers doubles, or of one without an ensemble), without the
+// graph and without advancing the clock.  keep (if non-null) receives the primitives of
+// every stage input over the entire domain, stepper_field_doubles(s) doubles per stage, in
+// block order; a floor fired in any stage is OR-ed into *floor_flag (if non-null).
+cudaError_t stepper_step_dt(aph_stepper s, const double *dt_dev, double *keep, int *floor_flag,
+                            cudaStream_t st);
+size_t stepper_field_doubles(aph_stepper s);
+
 // field: 0 cons, 1 u1
 cudaError_t launch_fill_ghosts(const PackDev &p, const BlockDev *blocks, int max_ncell, int field,
                                cudaStream_t s);

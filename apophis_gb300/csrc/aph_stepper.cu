@@ -393,7 +393,49 @@ void free_all(aph_stepper s) {
   cudaFree(s->d_members);
 }
 
+__global__ void k_set_dt(StepCtl *c, MemberCtl *m, int n, const double *dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!m) {
+    if (i == 0) c->dt = dt[0];
+    return;
+  }
+  if (i < n) {  // a member with dt 0 (past its end time) is skipped
+    m[i].dt = dt[i];
+    m[i].active = dt[i] > 0.0;
+  }
+}
+
+__global__ void k_or_flags(const int *flags, int n, int *out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (flags[i]) atomicOr(out, 1);
+}
+
 }  // namespace
+
+namespace aph {
+size_t stepper_field_doubles(aph_stepper s) { return (size_t)5 * s->total_cells; }
+
+cudaError_t stepper_step_dt(aph_stepper s, const double *dt_dev, double *keep, int *floor_flag,
+                            cudaStream_t st) {
+  const std::vector<Stage> stages = stages_of(s->integrator);
+  const int n = s->d_members ? s->nmembers : 1;
+  k_set_dt<<<(n + 127) / 128, 128, 0, st>>>(s->d_ctl, s->d_members, n, dt_dev);
+  cudaError_t e = cudaGetLastError();
+  const size_t field = stepper_field_doubles(s);
+  for (size_t i = 0; i < stages.size() && e == cudaSuccess; ++i) {
+    const int recon = (s->integrator == APH_INTEGRATOR_VL2 && i == 0) ? APH_RECON_DC : s->params.recon;
+    const StageArgs a = stage_args(s, (int)i, stages[i], false, false);
+    e = launch_one(s, a, recon, st);
+    if (e == cudaSuccess && keep)
+      e = cudaMemcpyAsync(keep + i * field, s->d_prim, field * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess && floor_flag) {
+      k_or_flags<<<(s->dev.nblocks + 255) / 256, 256, 0, st>>>(s->d_flags, s->dev.nblocks, floor_flag);
+      e = cudaGetLastError();
+    }
+  }
+  return e;
+}
+}  // namespace aph
 
 extern "C" {
 

@@ -127,16 +127,7 @@ class EnsembleStepper(_StepperBase):
             blocks[b].cons = self.cons.data_ptr() + 8 * 5 * ens.offset[b]
             blocks[b].nx[:] = [B.nx[0], B.nx[1], 1]
             blocks[b].dx[:] = [B.dx[0], B.dx[1], 1.0]
-        table = (_capi.aph_amr_block * nb)()
-        for b, B in enumerate(blks):
-            t = table[b]
-            t.level = B.level
-            t.origin[0], t.origin[1] = B.origin
-            for f in range(4):
-                t.face_kind[f] = B.face_kind[f]
-                t.face_count[f] = len(B.face_nbr[f])
-                for k, x in enumerate(B.face_nbr[f]):
-                    t.face_nbr[f][k] = x
+        table = self.face_table(blks)
         self._member = (ctypes.c_int * nb)(*ens.member_of)
         self._gm1 = (ctypes.c_double * ens.nmembers)(*[c.gm1 for c in ens.members])
         self._tlim = (ctypes.c_double * ens.nmembers)(*ens.tlim)
@@ -159,6 +150,21 @@ class EnsembleStepper(_StepperBase):
         desc.ensemble = ctypes.pointer(self._ens)
         self.h = ctypes.c_void_p()
         _capi.call("aph_stepper_create", ctypes.byref(desc), ctypes.byref(self.h))
+
+    @staticmethod
+    def face_table(blks):
+        from . import _capi
+        table = (_capi.aph_amr_block * len(blks))()
+        for b, B in enumerate(blks):
+            t = table[b]
+            t.level = B.level
+            t.origin[0], t.origin[1] = B.origin
+            for f in range(4):
+                t.face_kind[f] = B.face_kind[f]
+                t.face_count[f] = len(B.face_nbr[f])
+                for k, x in enumerate(B.face_nbr[f]):
+                    t.face_nbr[f][k] = x
+        return table
 
     def member_status(self):
         from . import _capi

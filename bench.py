@@ -257,6 +257,59 @@ def ensemble_leg(args):
             "end_time_min_max": [min(ms["time"]), max(ms["time"])]}
 
 
+def ensemble_adjoint_leg(ckpt=20):
+    """The blast ensemble's reverse sweep with respect to every member's initial state (the
+    gradient with respect to initial pressure is lambda_E / (gamma - 1) of it), all members
+    in the same launches: the members' dt schedules are recorded from a forward run to
+    t = 0.1, then the checkpointed rollout and its reverse sweep are timed (rank 0)."""
+    import torch
+    from apophis_gb300 import ensemble
+    from apophis_gb300.adjoint import EnsembleAdjoint
+    ens, flat = ensemble.blast_ensemble()
+    st = ensemble.EnsembleStepper(ens, flat, exact=False)
+    st.autotune(trial_steps=1)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    a, b = ev(), ev()
+    torch.cuda.synchronize()
+    a.record()
+    st.run_to_end(chunk=16)
+    b.record()
+    torch.cuda.synchronize()
+    fwd_s = a.elapsed_time(b) / 1e3
+    st.close()
+    st = ensemble.EnsembleStepper(ens, flat, exact=False)
+    dts = []
+    while True:
+        ms = st.member_status()
+        if max(ms["dt"]) == 0.0:
+            break
+        dts.append(ms["dt"])
+        st.step(1)
+    st.close()
+    del st
+    torch.cuda.empty_cache()
+    adj = EnsembleAdjoint(ens)
+    u0 = torch.from_numpy(flat).cuda()
+    a, b, c = ev(), ev(), ev()
+    a.record()
+    uT = adj.forward_members(u0, dts, ckpt)
+    b.record()
+    lam = torch.zeros_like(uT)
+    lam.copy_(uT)  # d(0.5 |U(T)|^2)/dU(T)
+    lam0 = adj.backward(lam)
+    c.record()
+    torch.cuda.synchronize()
+    ok = bool(torch.isfinite(lam0).all())
+    tape_s, bwd_s = a.elapsed_time(b) / 1e3, b.elapsed_time(c) / 1e3
+    adj.close()
+    return {"workload": "64-member blast ensemble to t = 0.1 (%d steps), PPM+HLLC, RK2, "
+                        "checkpoint every %d" % (len(dts), ckpt),
+            "forward_s": fwd_s, "checkpointed_forward_s": tape_s, "backward_s": bwd_s,
+            "ratio": bwd_s / fwd_s, "finite": ok,
+            "note": "backward includes the recomputation of each checkpoint segment; forward "
+                    "is the batched stepper run to t = 0.1"}
+
+
 def adjoint_leg(nsteps=40):
     """Adjoint/forward time ratio on the differentiable rollout (rank 0)."""
     import torch
@@ -452,6 +505,8 @@ def main():
         line["ensemble"] = ensemble_leg(args)
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = adjoint_leg()
+        if not args.no_ensemble:
+            line["ensemble_adjoint"] = ensemble_adjoint_leg()
     if rank == 0 and not args.no_cpu:
         zps, cores, el = cpu_baseline(cfg, cons, 1)
         line["cpu_baseline"] = {"value": zps, "unit": UNIT, "cores": cores, "kind": "port",

@@ -249,14 +249,17 @@ aph_status aph_stepper_autotune(aph_stepper stepper, int trial_steps, aph_steppe
                                 double *best_ms);
 
 /* ---- adjoint of the step --------------------------------------------------------------
- * Hand-written reverse mode of the full fixed-dt step: ConsToPrim, the PLM (or donor-cell)
- * limiter, the HLLE / HLLC fluxes with their wave-speed and contact branches, the flux
- * divergence, the RK stage combination and the ghost map.  No counterpart in the
- * reference (which has no derivatives); it differentiates the path the entry points above
- * implement.  All state arguments are device arrays in pack layout: nblocks consecutive
- * meshblocks of (5, nk, nj, ni) doubles, ghost entries ignored on input and zero in
- * adjoint outputs.  The pack is described by an aph_stepper_desc (its cons pointers are
- * not used: the adjoint owns its buffers); dc or plm, hlle or hllc, no gravity, nvar 5. */
+ * Hand-written reverse mode of the full fixed-dt step: ConsToPrim, the PPM, PLM or
+ * donor-cell limiters (each branch's transposed linear map; the quotient rule for PPM's
+ * extremum ratio), the HLLE / HLLC fluxes with their wave-speed and contact branches, the
+ * flux divergence, the RK stage combination and the ghost map.  No counterpart in the
+ * reference (which has no derivatives); it differentiates the step the batched stepper
+ * takes (its forward runs on an internal stepper).  All state arguments are device arrays
+ * in pack layout: nblocks consecutive meshblocks of (5, nk, nj, ni) doubles (blocks of equal
+ * size), ghost entries ignored on input and zero in adjoint outputs.  The pack is described
+ * by an aph_stepper_desc (its cons pointers are not used: the adjoint owns its buffers),
+ * uniform grids or face tables without coarse-fine faces, ensembles included; hlle or hllc,
+ * no gravity, nvar 5, fast arithmetic. */
 typedef struct aph_adjoint_s *aph_adjoint;
 aph_status aph_adjoint_create(const aph_stepper_desc *desc, aph_adjoint *out);
 aph_status aph_adjoint_destroy(aph_adjoint adjoint);
@@ -271,6 +274,11 @@ aph_status aph_adjoint_step_vjp(aph_adjoint adjoint, const double *u_n, double d
  * checkpoint every checkpoint_every steps on the device; writes the final state. */
 aph_status aph_adjoint_forward(aph_adjoint adjoint, const double *u0, int nsteps, const double *dts,
                                int checkpoint_every, double *u_final, void *stream);
+/* The same with a dt per member and step: dts[k * nmembers + m] (one member without an
+ * ensemble); aph_adjoint_forward uses dts[k] for every member. */
+aph_status aph_adjoint_forward_members(aph_adjoint adjoint, const double *u0, int nsteps,
+                                       const double *dts, int checkpoint_every, double *u_final,
+                                       void *stream);
 /* Reverse sweep of the last rollout: recompute each segment from its checkpoint, then the
  * step VJPs backwards; lam_initial = (dU^N/dU^0)^T lam_final (blocking). */
 aph_status aph_adjoint_backward(aph_adjoint adjoint, const double *lam_final, double *lam_initial,

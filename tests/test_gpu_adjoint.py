@@ -64,14 +64,15 @@ class Rollout(torch.autograd.Function):
 
 
 def kh_setup(n, block, rs, integ, recon="plm"):
-    cfg, cons = problems.kh2d_smooth(n=n, block=block, ng=2, recon=recon, rsolver=rs,
-                                     integrator=integ)
+    cfg, cons = problems.kh2d_smooth(n=n, block=block, ng=4 if recon == "ppm" else 2, recon=recon,
+                                     rsolver=rs, integrator=integ)
     return cfg, torch.from_numpy(cons).cuda()
 
 
 @pytest.mark.parametrize("rs,integ,recon", [("hlle", "rk2", "plm"), ("hllc", "rk2", "plm"),
                                             ("hlle", "vl2", "plm"), ("hllc", "rk3", "plm"),
-                                            ("hlle", "rk1", "dc")])
+                                            ("hlle", "rk1", "dc"), ("hllc", "rk2", "ppm"),
+                                            ("hlle", "rk3", "ppm")])
 def test_step_vjp_matches_taped_reference(cuda, rs, integ, recon):
     cfg, u = kh_setup(64, 32, rs, integ, recon)
     adj = Adjoint(cfg)

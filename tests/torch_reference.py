@@ -1,8 +1,8 @@
 """PyTorch FP64 restatement of the fixed-dt hydro step on a periodic global grid, for the
 taped reference gradient of the adjoint tests (test infrastructure only).
 
-It follows the same formulas as the CUDA fast path: ConsToPrim, PLM (plm_simple.hpp:15-32)
-or donor cell, HLLE (hydro_hlle.hpp:28-133) or HLLC (hydro_hllc.hpp:161-282) with the
+It follows the same formulas as the CUDA fast path: ConsToPrim, PPM (ppm_simple.hpp:32-161),
+PLM (plm_simple.hpp:15-32) or donor cell, HLLE (hydro_hlle.hpp:28-133) or HLLC (hydro_hllc.hpp:161-282) with the
 c-limited sound speed written as sqrt(C^2 gamma p / (p (1 + 1/gm1) + rho C^2)), the flux
 divergence and the low-storage RK stages.  torch.autograd differentiates it.
 """
@@ -33,11 +33,63 @@ def prim_to_cons(W, gm1):
     return torch.cat([rho[None], m, E[None]], 0)
 
 
-def _recon(q, recon, axis):
-    """q padded by 2 cells along axis (cells -2..n+1); returns left/right face states
-    for faces 0..n: left from cell f-1, right from cell f."""
-    n = q.shape[axis] - 4
-    sl = lambda a, b: q.narrow(axis, a + 2, b - a)  # cells a..b-1
+def _ppm(q, axis, G):
+    """PPM face states (the face/cell split of the CUDA path, with its limiter branches)."""
+    n = q.shape[axis] - 2 * G
+    sl = lambda a, b: q.narrow(axis, a + G, b - a)  # cells a..b-1
+    C2 = 1.25
+    Q4 = sl(-2, n + 2)                        # cells -2..n+1
+    qm, qp = sl(-3, n + 1), sl(-1, n + 3)
+    dd = 0.5 * (qp - Q4) + 0.5 * (Q4 - qm)
+    d2 = (qm + qp) - 2.0 * Q4
+    nf = n + 3                                # faces -1..n+1: between cells f-1 and f
+    qm1, q0 = Q4.narrow(axis, 0, nf), Q4.narrow(axis, 1, nf)
+    ddm1, dd0 = dd.narrow(axis, 0, nf), dd.narrow(axis, 1, nf)
+    d2m1, d20 = d2.narrow(axis, 0, nf), d2.narrow(axis, 1, nf)
+    avg = 0.5 * (qm1 + q0)
+    dph = avg + (ddm1 - dd0) / 6.0
+    qa_tmp, qb_tmp = dph - qm1, q0 - dph
+    qa = 3.0 * (qm1 + q0 - 2.0 * dph)
+    sa = qa < 0
+    match = (sa == (d2m1 < 0)) & (sa == (d20 < 0))
+    m = C2 * torch.where(d20.abs() < d2m1.abs(), d20.abs(), d2m1.abs())
+    qd_mag_is_qa = qa.abs() < m
+    qd = torch.where(qd_mag_is_qa, qa, torch.where(sa, -m, m))
+    qd = torch.where(match, qd, torch.zeros_like(qd))
+    dph = torch.where(qa_tmp * qb_tmp < 0, avg - qd / 6.0, dph)
+    nc = n + 2                                # cells -1..n
+    lo, hi = dph.narrow(axis, 0, nc), dph.narrow(axis, 1, nc)
+    qim2, qim1, qi, qip1, qip2 = (sl(-3, n - 1), sl(-2, n), sl(-1, n + 1), sl(0, n + 2),
+                                  sl(1, n + 3))
+    e2m1, e20, e2p1 = d2.narrow(axis, 0, nc), d2.narrow(axis, 1, nc), d2.narrow(axis, 2, nc)
+    d2qf = 6.0 * (lo + hi - 2.0 * qi)
+    dqm, dqp = qi - lo, hi - qi
+    ext = ~(dqm * dqp > 0) | ~((qip1 - qi) * (qi - qim1) > 0)
+    sd = d2qf < 0
+    smatch = (sd == (e2m1 < 0)) & (sd == (e20 < 0)) & (sd == (e2p1 < 0))
+    mm = torch.minimum(torch.minimum(e2m1.abs(), e20.abs()), e2p1.abs()) * C2
+    qe_mag = torch.where(d2qf.abs() < mm, d2qf.abs(), mm)
+    qe = torch.where(smatch, torch.where(sd, -qe_mag, qe_mag), torch.zeros_like(qe_mag))
+    mx = torch.stack([qim2.abs(), qim1.abs(), qi.abs(), qip1.abs(), qip2.abs()]).amax(0)
+    big = d2qf.abs() > 1e-12 * mx
+    rho = torch.where(big, qe / torch.where(big, d2qf, torch.ones_like(d2qf)), torch.zeros_like(d2qf))
+    app = rho <= 1.0 - 1e-12
+    qr_e = torch.where(app, qi - rho * dqm, lo)
+    ql_e = torch.where(app, qi + rho * dqp, hi)
+    qr_m = torch.where(dqm.abs() >= 2.0 * dqp.abs(), qi - 2.0 * dqp, lo)
+    ql_m = torch.where(dqp.abs() >= 2.0 * dqm.abs(), qi + 2.0 * dqm, hi)
+    ql = torch.where(ext, ql_e, ql_m)
+    qr = torch.where(ext, qr_e, qr_m)
+    return ql.narrow(axis, 0, n + 1), qr.narrow(axis, 1, n + 1)
+
+
+def _recon(q, recon, axis, G=2):
+    """q padded by G cells along axis; returns left/right face states for faces 0..n: left
+    from cell f-1, right from cell f."""
+    if recon == "ppm":
+        return _ppm(q, axis, G)
+    n = q.shape[axis] - 2 * G
+    sl = lambda a, b: q.narrow(axis, a + G, b - a)  # cells a..b-1
     if recon == "dc":
         return sl(-1, n), sl(0, n + 1)
     qm, q0, qp = sl(-2, n), sl(-1, n + 1), sl(0, n + 2)  # around cells -1..n
@@ -131,10 +183,11 @@ def rhs(U, dx, gamma, recon, rsolver, ndim):
     """R(U) = -div F on a periodic global grid U (5, NZ, NY, NX)."""
     gm1 = gamma - 1.0
     axes = [3, 2, 1][:ndim]  # x, y, z axes of (var, z, y, x)
+    G = 3 if recon == "ppm" else 2
     pad = U
     for ax in axes:
         n = pad.shape[ax]
-        pad = torch.cat([pad.narrow(ax, n - 2, 2), pad, pad.narrow(ax, 0, 2)], ax)
+        pad = torch.cat([pad.narrow(ax, n - G, G), pad, pad.narrow(ax, 0, G)], ax)
     W = c2p(pad, gm1)
     out = torch.zeros_like(U)
     solve = hlle if rsolver == "hlle" else hllc
@@ -143,8 +196,8 @@ def rhs(U, dx, gamma, recon, rsolver, ndim):
         Wd = W
         for od, oax in enumerate(axes):
             if oax != ax:
-                Wd = Wd.narrow(oax, 2, Wd.shape[oax] - 4)
-        L, R = _recon(Wd, recon, ax)
+                Wd = Wd.narrow(oax, G, Wd.shape[oax] - 2 * G)
+        L, R = _recon(Wd, recon, ax, G)
         ivx = 1 + d
         ivy = 1 + (d + 1) % 3
         ivz = 1 + (d + 2) % 3
