@@ -105,6 +105,21 @@ __device__ __forceinline__ bool cons_to_prim_cell(double *u, double *w, double &
   w[IV3] = u[IM3] * di;
   const double e_k = 0.5 * di * (u[IM1] * u[IM1] + u[IM2] * u[IM2] + u[IM3] * u[IM3]);
   double u_e = u[IEN];
+#if !APH_EXACT
+  // fast: p = gm1 rho ((E - e_k) / rho) = gm1 (E - e_k), and with the floors inactive both
+  // adiabatic indices are gamma (B / p = gm1 + 1 = p / (rho e) + 1), so one division per cell
+  {
+    const double pe = gm1 * (u_e - e_k);
+    const double wp = is_neg(pe) ? 0.0 : pe;
+    if (gt(wp, pfloor)) {
+      u[IEN] = u_e;
+      w[IPR] = wp;
+      g_c = gm1 + 1.0;
+      g_e = g_c;
+      return false;
+    }
+  }
+#endif
   double w_p = eos_pressure(gm1, u_d, (u_e - e_k) / u_d);
   const bool floored = !gt(w_p, pfloor);
   if (floored) {
@@ -402,6 +417,30 @@ __device__ __forceinline__ void solve_hllc(const double *wli, const double *wri,
   double cp = (ml * tr + mr * tl) * imm;
 #endif
   cp = is_pos(cp) ? cp : 0.0;
+#if !APH_EXACT
+  {
+    // one-sided: the flux is sstar/(sstar - b) times the physical flux of the upwind side of
+    // the contact (left with b = bm when sstar >= 0, else right with b = bp) plus the
+    // pressure terms; the other side's weight is exactly 0, so this is the two-sided sum of
+    // the reference with its zero term dropped
+    const bool L = !is_neg(sstar);
+    const double rho = L ? wli[IDN] : wri[IDN], u = L ? wli[IV1] : wri[IV1];
+    const double v = L ? wli[IV2] : wri[IV2], z = L ? wli[IV3] : wri[IV3];
+    const double p = L ? wli[IPR] : wri[IPR];
+    const double b = L ? bm : bp;
+    const double e = p * (L ? igm1l : igm1r) + 0.5 * rho * (u * u + v * v + z * z);
+    const double id = 1.0 / (sstar - b);
+    const double coef = sstar * id;
+    const double ustar = -b * id;
+    const double vx = u - b;
+    flxi[IDN] = coef * (rho * vx);
+    flxi[IV1] = coef * (rho * u * vx + p) + ustar * cp;
+    flxi[IV2] = coef * (rho * v * vx);
+    flxi[IV3] = coef * (rho * z * vx);
+    flxi[IEN] = coef * (e * vx + p * u) + ustar * cp * sstar;
+    return;
+  }
+#endif
   vxl = wli[IV1] - bm;
   vxr = wri[IV1] - bp;
   double fl[NHYDRO], fr[NHYDRO];
@@ -461,7 +500,7 @@ __device__ __forceinline__ void riemann(const double *wl, const double *wr, doub
 }
 
 // EstimateTimestep per-cell candidate (hydro.cpp:384-415): min over active directions
-// of dx_d / (|v_d| + lambda).
+// of dx_d / (|v_d| + lambda).  dt_cell below is the form the stage kernel uses.
 __device__ __forceinline__ double dt_candidate(const double *w, double e_cons, const double *dx,
                                                int ndim, double gm1) {
   const double e_internal =
@@ -479,6 +518,30 @@ __device__ __forceinline__ double dt_candidate(const double *w, double e_cons, c
     m = lt(c3, m) ? c3 : m;
   }
   return m;
+}
+
+// dt candidate of a cell just converted by cons_to_prim_cell (floored: its return value).
+// Fast mode with the floors inactive: lambda is the c-limited sound speed of the constant
+// gamma (the same quantity: rho e = p / gm1), and one reciprocal of the largest rate
+// (|v_d| + lambda) / dx_d replaces a division per direction.
+__device__ __forceinline__ double dt_cell(const double *w, double e_cons, const double *dx, int ndim,
+                                          const GasConsts &gc, bool floored) {
+#if APH_EXACT
+  return dt_candidate(w, e_cons, dx, ndim, gc.gm1);
+#else
+  if (floored) return dt_candidate(w, e_cons, dx, ndim, gc.gm1);
+  const double lam = sound_speed<true>(w[IDN], w[IPR], 0.0, 0.0, gc);
+  double r = (dabs(w[IV1]) + lam) / dx[0];
+  if (ndim > 1) {
+    const double r2 = (dabs(w[IV2]) + lam) / dx[1];
+    r = lt(r, r2) ? r2 : r;
+  }
+  if (ndim > 2) {
+    const double r3 = (dabs(w[IV3]) + lam) / dx[2];
+    r = lt(r, r3) ? r3 : r;
+  }
+  return 1.0 / r;
+#endif
 }
 
 }  // namespace aph

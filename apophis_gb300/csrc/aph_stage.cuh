@@ -406,6 +406,9 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
       }
     } else {
       const double vol = B.dx[0] * B.dx[1] * B.dx[2];
+#if !APH_EXACT
+      const double ivol = 1.0 / vol;
+#endif
       const double beta_dt = a.beta * dt_of(a, B);
       unsigned long long mymin = ~0ULL;
       for (int it = tid; it < nl * n; it += nth) {
@@ -420,7 +423,11 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
           const size_t of = v * fs + (size_t)t * w1 + c;
           double du = (area * F[of + 1] - area * F[of]);
           if (!first_pass) du = B.du[v * B.nint + icell] + du;
+#if APH_EXACT
           const double div = -du / vol;
+#else
+          const double div = -du * ivol;
+#endif
           u[v] = a.gam0 * B.u0[v * nc + cell] + a.gam1 * B.u1[v * nc + cell] + beta_dt * div;
         }
         if (a.gravity) {  // ApplyGravity with the stage input's prim (gravity.cpp:386-407)
@@ -441,8 +448,8 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
         for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + cell] = u[v];
         if (a.last) {  // EstimateTimestep on the floored new state
           double w[NHYDRO], gcc, gce;
-          cons_to_prim_cell(u, w, gcc, gce, gc.gm1, a.p.dfloor, a.p.pfloor);
-          const unsigned long long b = dt_bits(dt_candidate(w, u[IEN], B.dx, a.p.ndim, gc.gm1));
+          const bool fl = cons_to_prim_cell(u, w, gcc, gce, gc.gm1, a.p.dfloor, a.p.pfloor);
+          const unsigned long long b = dt_bits(dt_cell(w, u[IEN], B.dx, a.p.ndim, gc, fl));
           mymin = b < mymin ? b : mymin;
         }
       }
