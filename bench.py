@@ -56,8 +56,9 @@ WORKLOAD = ("kh3d 256^3: 64 meshblocks of 64^3, 4 ghost cells, PPM+HLLC, RK2, CF
             "gamma 5/3, FP64")
 BYTES_PER_ZONE_UPDATE = 200.0   # RK2 with 5 FP64 conserved variables
 # FP64 work of the stage kernel (fast mode) per RK2 zone-update: DADD + DMUL + DFMA thread
-# instructions from the ncu capture in profiles/stage_kernel_kh3d.md (1,298 per zone per stage)
-FP64_LANE_OPS_PER_ZONE_UPDATE = 2597.0
+# instructions from the ncu capture in profiles/stage_kernel_kh3d.md (1,160 in the stage with
+# the dt epilogue + 1,104 in the other, per zone)
+FP64_LANE_OPS_PER_ZONE_UPDATE = 2264.0
 FP64_LANES_PER_CLK_PER_SM = 2.0    # DFMA lanes per clock per SM on GB300 (profiles/fp64_pipe_gb300.md)
 # DRAM bytes (read + write) per zone per stage launch, same capture (128^3 pack of 64^3 blocks;
 # the 256^3 launches process the same blocks, 8x as many)
@@ -182,49 +183,50 @@ def amr_leg(args, warmup):
            "batched": {"value": zones / (bms * 1e-3), "ms_per_step": bms, "steps": nsteps,
                        "stage_ms": stage_ms, "launches_per_step": 3,
                        "launch": tune["config"] if tune else None, "sim_time": status["time"]}}
-    drv = amr.AmrDriver(cfg, cons, exact=False)
-    drv.run(nsteps=2)
-    pms = timed(lambda n: drv.run(nsteps=n), 20)
-    out["plain_per_pack"] = {"value": zones / (pms * 1e-3), "ms_per_step": pms}
-    drv.md.close()
-    del drv
-    # per meshblock, host-driven: each kernel launched once per block through the C ABI
-    drv = amr.AmrDriver(cfg, cons, exact=False, per_block=True)
-    drv.run(nsteps=1)
-    hms = timed(lambda n: drv.run(nsteps=n), 2)
-    # the same launches replayed from one CUDA graph (no host cost): fixed dt, each block's
-    # dt estimate written to the device
-    dts = torch.empty(cfg.nblocks, dtype=torch.float64, device="cuda")
-    from apophis_gb300 import _capi
+    if not args.no_plain:
+        drv = amr.AmrDriver(cfg, cons, exact=False)
+        drv.run(nsteps=2)
+        pms = timed(lambda n: drv.run(nsteps=n), 20)
+        out["plain_per_pack"] = {"value": zones / (pms * 1e-3), "ms_per_step": pms}
+        drv.md.close()
+        del drv
+        # per meshblock, host-driven: each kernel launched once per block through the C ABI
+        drv = amr.AmrDriver(cfg, cons, exact=False, per_block=True)
+        drv.run(nsteps=1)
+        hms = timed(lambda n: drv.run(nsteps=n), 2)
+        # the same launches replayed from one CUDA graph (no host cost): fixed dt, each block's
+        # dt estimate written to the device
+        dts = torch.empty(cfg.nblocks, dtype=torch.float64, device="cuda")
+        from apophis_gb300 import _capi
 
-    def body():
-        drv.step(1e-5)
-        for b, p in enumerate(drv.md.block_packs):
-            _capi.call("aph_hydro_estimate_timestep_async", p,
-                       ctypes.c_void_p(dts.data_ptr() + 8 * b), hydro.stream_handle())
-    side = torch.cuda.Stream()
-    side.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(side):
-        body()
-    torch.cuda.current_stream().wait_stream(side)
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
-        body()
-    g.replay()
-    gms = timed(lambda n: [g.replay() for _ in range(n)], 10)
-    launches = cfg.nblocks * (2 * 5 + 3) + 2
-    out["plain_per_meshblock"] = {"value": zones / (hms * 1e-3), "ms_per_step": hms,
-                                  "launches_per_step": launches, "driver": "host (ctypes)"}
-    out["plain_per_meshblock_graph"] = {"value": zones / (gms * 1e-3), "ms_per_step": gms,
-                                        "launches_per_step": launches,
-                                        "driver": "one CUDA graph per step"}
-    del g
-    drv.md.close()
-    del drv
-    torch.cuda.empty_cache()
-    out["batched_vs_plain_per_meshblock_graph"] = gms / bms
-    out["batched_vs_plain_per_meshblock"] = hms / bms
-    out["batched_vs_plain_per_pack"] = pms / bms
+        def body():
+            drv.step(1e-5)
+            for b, p in enumerate(drv.md.block_packs):
+                _capi.call("aph_hydro_estimate_timestep_async", p,
+                           ctypes.c_void_p(dts.data_ptr() + 8 * b), hydro.stream_handle())
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            body()
+        torch.cuda.current_stream().wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            body()
+        g.replay()
+        gms = timed(lambda n: [g.replay() for _ in range(n)], 10)
+        launches = cfg.nblocks * (2 * 5 + 3) + 2
+        out["plain_per_meshblock"] = {"value": zones / (hms * 1e-3), "ms_per_step": hms,
+                                      "launches_per_step": launches, "driver": "host (ctypes)"}
+        out["plain_per_meshblock_graph"] = {"value": zones / (gms * 1e-3), "ms_per_step": gms,
+                                            "launches_per_step": launches,
+                                            "driver": "one CUDA graph per step"}
+        del g
+        drv.md.close()
+        del drv
+        torch.cuda.empty_cache()
+        out["batched_vs_plain_per_meshblock_graph"] = gms / bms
+        out["batched_vs_plain_per_meshblock"] = hms / bms
+        out["batched_vs_plain_per_pack"] = pms / bms
     bytes_per_launch = BYTES_PER_ZONE_UPDATE * zones / len(stage_ms)
     out["hbm_achieved_gbs"] = bytes_per_launch / (sum(stage_ms) / len(stage_ms) * 1e-3) / 1e9
     return out
@@ -381,8 +383,19 @@ def main():
     ap.add_argument("--no-amr", action="store_true", help="skip the refined-pack leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint ratio leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the blast-ensemble leg")
+    ap.add_argument("--only", choices=["amr", "ensemble", "adjoint"],
+                    help="run one extra leg alone and print its object (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        from apophis_gb300 import _build
+        _build.build()
+        out = {"amr": lambda: amr_leg(args, args.warmup), "ensemble": lambda: ensemble_leg(args),
+               "adjoint": adjoint_leg}[args.only]()
+        print(json.dumps({"only": args.only, args.only: out}), flush=True)
+        return
 
     from apophis_gb300 import problems
     cfg, cons = problems.kh3d(n=args.n, block=64 if args.n >= 64 else args.n // 2, ng=4)
