@@ -33,6 +33,7 @@ UNITS = {
     "aph_stepper.cu": [],
     "aph_adjoint.cu": [],
     "aph_noalloc.cu": [],
+    "aph_history.cu": [],
 }
 
 

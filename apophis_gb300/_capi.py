@@ -119,6 +119,8 @@ SIGNATURES = {
     "aph_stepper_step": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_status": ([ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int),
                             ctypes.c_void_p], ctypes.c_int),
+    "aph_hydro_history": ([ctypes.c_void_p, _dp, ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_history": ([ctypes.c_void_p, _dp, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_member_status": ([ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int),
                                    ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_get_config": ([ctypes.c_void_p, ctypes.POINTER(aph_stepper_config)],

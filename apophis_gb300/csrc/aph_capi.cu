@@ -74,6 +74,8 @@ struct aph_pack_s {
   BlockDev *d_blocks = nullptr;
   unsigned long long *d_scratch = nullptr;  // [0] dt min bits, [1] floor flag
   double *d_dt = nullptr;
+  double *d_hist = nullptr;  // history partial sums (allocated on first use)
+  size_t hist_len = 0;
   int max_ncell = 0, max_interior = 0;
   bool uniform = true;
   bool has_topology = false;
@@ -352,6 +354,7 @@ aph_status aph_pack_destroy(aph_pack p) {
   if (p->d_blocks) cudaFree(p->d_blocks);
   if (p->d_scratch) cudaFree(p->d_scratch);
   if (p->d_dt) cudaFree(p->d_dt);
+  if (p->d_hist) cudaFree(p->d_hist);
   delete p;
   return APH_OK;
 }
@@ -460,6 +463,26 @@ aph_status aph_hydro_estimate_timestep(aph_pack p, double *dt_host, void *stream
   cudaError_t e = cudaMemcpyAsync(dt_host, p->d_dt, sizeof(double), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return e == cudaSuccess ? APH_OK : cuda_fail(e, "estimate_timestep");
+}
+
+aph_status aph_hydro_history(aph_pack p, double out[2], void *stream) {
+  clear_error();
+  if (!p || !out) return fail(APH_ERR_INVALID, "NULL argument");
+  const size_t need = history_scratch_doubles(p->max_interior, p->dev.nblocks);
+  if (p->hist_len < need) {
+    if (p->d_hist) cudaFree(p->d_hist);
+    p->d_hist = nullptr;
+    p->hist_len = 0;
+    cudaError_t e = cudaMalloc(&p->d_hist, need * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(e, "history scratch");
+    p->hist_len = need;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  double *res = p->d_hist + need - 2;
+  cudaError_t e = launch_history(p->dev, p->d_blocks, p->max_interior, p->d_hist, need - 2, res, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, res, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "history");
 }
 
 aph_status aph_hydro_apply_gravity(aph_pack p, const double g[3], double beta_dt, void *stream) {

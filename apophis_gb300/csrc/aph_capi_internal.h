@@ -31,6 +31,14 @@ cudaError_t stepper_step_dt(aph_stepper s, const double *dt_dev, double *keep, i
                             cudaStream_t st);
 size_t stepper_field_doubles(aph_stepper s);
 
+// History sums (aph_history.cu): out_dev[0] total mass, out_dev[1] total energy; scratch
+// needs history_scratch_doubles(max_interior, nblocks) doubles (the last two hold the result).
+size_t history_scratch_doubles(int max_interior, int nblocks);
+cudaError_t launch_history(const PackDev &p, const BlockDev *blocks, int max_interior, double *scratch,
+                           size_t scratch_len, double *out_dev, cudaStream_t s);
+cudaError_t launch_history_steps(const PackDev &p, const StepBlock *blocks, int max_interior,
+                                 double *scratch, size_t scratch_len, double *out_dev, cudaStream_t s);
+
 // field: 0 cons, 1 u1
 cudaError_t launch_fill_ghosts(const PackDev &p, const BlockDev *blocks, int max_ncell, int field,
                                cudaStream_t s);

@@ -171,6 +171,8 @@ struct aph_stepper_s {
   std::vector<std::vector<double *>> u0_ptrs;
   MemberCtl *d_members = nullptr;  // ensembles
   int nmembers = 0;
+  double *d_hist = nullptr;        // history partial sums (allocated on first use)
+  size_t hist_len = 0;
 };
 
 namespace {
@@ -391,6 +393,7 @@ void free_all(aph_stepper s) {
   cudaFree(s->d_fix_items);
   cudaFree(s->d_bflux);
   cudaFree(s->d_members);
+  cudaFree(s->d_hist);
 }
 
 __global__ void k_set_dt(StepCtl *c, MemberCtl *m, int n, const double *dt) {
@@ -737,6 +740,28 @@ aph_status aph_stepper_member_status(aph_stepper s, double *time, double *dt, in
   }
   StepCtl c;
   return read_ctl(s, &c);
+}
+
+aph_status aph_stepper_history(aph_stepper s, double out[2], void *stream) {
+  clear_error();
+  if (!s || !out) return fail(APH_ERR_INVALID, "NULL argument");
+  int max_int = 0;
+  for (const StepBlock &B : s->hblocks) max_int = std::max<int>(max_int, (int)B.nint);
+  const size_t need = history_scratch_doubles(max_int, s->dev.nblocks);
+  if (s->hist_len < need) {
+    cudaFree(s->d_hist);
+    s->d_hist = nullptr;
+    s->hist_len = 0;
+    cudaError_t e = cudaMalloc(&s->d_hist, need * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(e, "history scratch");
+    s->hist_len = need;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  double *res = s->d_hist + need - 2;
+  cudaError_t e = launch_history_steps(s->dev, s->d_blocks, max_int, s->d_hist, need - 2, res, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, res, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "stepper history");
 }
 
 aph_status aph_stepper_get_config(aph_stepper s, aph_stepper_config *cfg) {

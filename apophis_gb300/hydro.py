@@ -142,6 +142,13 @@ def ApplyGravity(md, g, beta_dt, pack=None, stream=None):
     _capi.call("aph_hydro_apply_gravity", pack or md.pack, ga, beta_dt, stream_handle(stream))
 
 
+def History(md, pack=None, stream=None):
+    """GlobalQuantHst (hydro.cpp:754-771): {"total_mass", "total_energy"} of the interiors."""
+    out = (ctypes.c_double * 2)()
+    _capi.call("aph_hydro_history", pack or md.pack, out, stream_handle(stream))
+    return {"total_mass": out[0], "total_energy": out[1]}
+
+
 def FillGhosts(md, stream=None):
     _capi.call("aph_hydro_fill_ghosts", md.pack, stream_handle(stream))
 

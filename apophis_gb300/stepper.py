@@ -73,6 +73,12 @@ class Stepper:
                    ctypes.byref(n), stream_handle(stream))
         return {"time": t.value, "dt": dt.value, "ncycle": n.value}
 
+    def history(self, stream=None):
+        """GlobalQuantHst of the state: {"total_mass", "total_energy"}."""
+        out = (ctypes.c_double * 2)()
+        _capi.call("aph_stepper_history", self.h, out, stream_handle(stream))
+        return {"total_mass": out[0], "total_energy": out[1]}
+
     def run(self, nsteps=1 << 30, tlim=float("inf"), check_every=16):
         """Step until nsteps or tlim (checking the device clock every check_every steps)."""
         done = 0

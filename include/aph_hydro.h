@@ -166,6 +166,12 @@ aph_status aph_hydro_estimate_timestep_noalloc(const double *prim, const double 
 
 /* ApplyGravity for a constant field g (src/gravity/gravity.cpp:374-410) with the
  * stage's beta*dt; uses prim of the previous FillDerived as the reference does. */
+/* History sums GlobalQuantHst<Sum, IDN> and <Sum, IEN> (src/hydro/hydro.cpp:336-346,
+ * 754-771), the hydro package's history outputs total_mass and total_energy: the sum over
+ * interior cells of cons * CellVolume; out[0] mass, out[1] energy (blocking).  Reduced in a
+ * fixed order, so repeated calls on the same state agree bit for bit. */
+aph_status aph_hydro_history(aph_pack pack, double out[2], void *stream);
+
 aph_status aph_hydro_apply_gravity(aph_pack pack, const double g[3], double beta_dt,
                                    void *stream);
 
@@ -238,6 +244,8 @@ aph_status aph_stepper_status(aph_stepper stepper, double *time, double *dt, int
  * member time, the largest next dt and the largest cycle count. */
 aph_status aph_stepper_member_status(aph_stepper stepper, double *time, double *dt, int *ncycle,
                                      void *stream);
+/* The history sums of the stepper's state (as aph_hydro_history, over all blocks). */
+aph_status aph_stepper_history(aph_stepper stepper, double out[2], void *stream);
 aph_status aph_stepper_get_config(aph_stepper stepper, aph_stepper_config *cfg);
 aph_status aph_stepper_set_config(aph_stepper stepper, const aph_stepper_config *cfg);
 /* Advance nsteps steps without the graph, timing each stage launch with CUDA events on

@@ -220,3 +220,13 @@ class AmrMesh:
         out = np.zeros(3)
         lib().orc_amr_state(self.h, _p(out))
         return {"time": out[0], "dt": out[1], "ncycle": int(out[2])}
+
+
+def history(cfg, cons):
+    """GlobalQuantHst<Sum, IDN / IEN> (src/hydro/hydro.cpp:754-771): the sums over interior
+    cells of cons * CellVolume, for a uniform pack (nblocks, nvar, nk, nj, ni)."""
+    sk, sj, si = cfg.interior
+    vol = float(np.prod(cfg.dx))
+    inner = np.asarray(cons)[:, :, sk, sj, si]
+    return {"total_mass": float(inner[:, 0].sum() * vol),
+            "total_energy": float(inner[:, 4].sum() * vol)}
