@@ -180,3 +180,15 @@ def test_face_table_check_rejects_bad_tables():
     t[fine].origin[1] += 1
     with pytest.raises(_capi.AphError):
         amr.check_table(cfg, t)
+
+
+def test_rt_amr_block_list_is_pinned():
+    """The RT pack's block list is deterministic: it equals the committed JSON."""
+    import json
+    import os
+    import sys
+    gold = os.path.join(os.path.dirname(__file__), "golden")
+    sys.path.insert(0, gold)
+    import make_rt_amr_blocks
+    want = json.load(open(os.path.join(gold, "rt2d_amr_blocks.json")))
+    assert make_rt_amr_blocks.block_list() == want
