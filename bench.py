@@ -354,6 +354,21 @@ def adjoint_leg(nsteps=40):
             "note": "backward includes the recomputation of each checkpoint segment"}
 
 
+def cpu_baseline_amr(nsteps=2):
+    """The refined-mesh oracle on the RT pack (host cores)."""
+    from apophis_gb300 import amr
+    from oracle import oracle as O
+    cfg, cons = amr.rt2d_amr()
+    m = O.AmrMesh(cfg)
+    m.set_cons(cons)
+    m.run(nsteps=1)
+    t0 = time.perf_counter()
+    m.run(nsteps=nsteps)
+    el = time.perf_counter() - t0
+    return {"value": cfg.zones() * nsteps / el, "unit": UNIT, "cores": O.num_threads(),
+            "kind": "port", "sample": "%d RK2 steps of the RT pack after 1 warm-up" % nsteps}
+
+
 def run_reference(args, cfg, cons):
     dist, rank, ws = dist_init()
     if rank != 0:
@@ -471,7 +486,22 @@ def main():
         torch.cuda.synchronize()
         pms = (time.perf_counter() - t0) * 1e3 / 2
         plain = {"value": zones / (pms * 1e-3), "ms_per_step": pms,
-                 "launches_per_step": 2 * cfg.nblocks * (1 + 3 + 1) + 2 + 2 + cfg.nblocks}
+                 "launches_per_step": 2 * cfg.nblocks * (1 + 3 + 1) + 2 + 2 + cfg.nblocks,
+                 "driver": "one launch per kernel per meshblock"}
+        del drv
+        torch.cuda.empty_cache()
+        # reference-style granularity: one launch per kernel per pack (the Kokkos kernels over a
+        # MeshBlockPack)
+        drv = hydro.Driver(cfg, cons, exact=False, per_block=False)
+        drv.run(nsteps=1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        drv.run(nsteps=2)
+        torch.cuda.synchronize()
+        kms = (time.perf_counter() - t0) * 1e3 / 2
+        plain_pack = {"value": zones / (kms * 1e-3), "ms_per_step": kms,
+                      "launches_per_step": 2 * (1 + 3 + 1) + 2 + 2 + 1,
+                      "driver": "one launch per kernel per pack"}
         del drv
         torch.cuda.empty_cache()
 
@@ -510,7 +540,9 @@ def main():
                                   "frac": ach / fp64_peak})
     if plain is not None:
         line["plain"] = plain
+        line["plain_per_pack"] = plain_pack
         line["batched_vs_plain"] = value / ws / plain["value"]
+        line["batched_vs_plain_per_pack"] = value / ws / plain_pack["value"]
     if rank == 0 and not args.no_amr:
         line["amr"] = amr_leg(args, args.warmup)
         line["gpu_launches_amr_batched_step"] = 3
@@ -521,10 +553,13 @@ def main():
         if not args.no_ensemble:
             line["ensemble_adjoint"] = ensemble_adjoint_leg()
     if rank == 0 and not args.no_cpu:
-        zps, cores, el = cpu_baseline(cfg, cons, 1)
+        runs = [cpu_baseline(cfg, cons, 1) for _ in range(3)]
+        zps, cores, el = sorted(runs)[1]
         line["cpu_baseline"] = {"value": zps, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": "1 full RK2 step of the 256^3 pack after 1 warm-up "
-                                          "(%.1f s)" % el}
+                                "sample": "median of 3 runs of 1 full RK2 step of the 256^3 pack, "
+                                          "each after 1 warm-up step (%.1f s per run)" % el}
+        if "amr" in line:
+            line["amr"]["cpu_baseline"] = cpu_baseline_amr()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
