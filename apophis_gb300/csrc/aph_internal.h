@@ -143,8 +143,10 @@ APH_DECLARE_LAUNCHERS(aph_exact)
   size_t stage_smem_bytes(int recon, int n, int T);                                            \
   const void *stage_kernel(int recon, int rsolver);                                            \
   cudaError_t launch_stage(const aph::StageArgs &a, int recon, int rsolver, int grid,          \
-                           int threads, size_t smem, bool cooperative, cudaStream_t s);        \
-  cudaError_t stage_occupancy(int recon, int rsolver, int threads, size_t smem, int *blocks);  \
+                           int threads, size_t smem, bool cooperative, int reg_cap,            \
+                           cudaStream_t s);                                                    \
+  cudaError_t stage_occupancy(int recon, int rsolver, int threads, size_t smem, int reg_cap,   \
+                              int *blocks);                                                    \
   }
 APH_DECLARE_STAGE(aph_fast)
 APH_DECLARE_STAGE(aph_exact)

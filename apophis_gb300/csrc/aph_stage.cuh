@@ -530,8 +530,10 @@ __device__ void amr_update(const StageArgs &a, const Sched &sched, unsigned int 
   }
 }
 
-template <int RECON, int RS>
-__global__ void __launch_bounds__(kStageThreads, 1) k_stage(StageArgs a) {
+// MINB: resident CTAs per SM the registers are budgeted for (1: as many registers as the code
+// wants; 3: capped near 80 per thread for 256-thread CTAs, trading a few spills for occupancy).
+template <int RECON, int RS, int MINB>
+__global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
   extern __shared__ double sm[];
   const PackDev &p = a.p;
   const Sched sched{a.schedule};
@@ -651,26 +653,31 @@ size_t stage_smem_bytes(int recon, int n, int T) {
   return pass_smem_doubles(recon, n, T, 7) * sizeof(double);
 }
 
-template <int RECON>
+template <int RECON, int MINB>
 static const void *kernel_for_rs(int rs) {
   switch (rs) {
-    case RS_HLLE: return (const void *)k_stage<RECON, RS_HLLE>;
-    case RS_HLLC: return (const void *)k_stage<RECON, RS_HLLC>;
-    case RS_LHLLC: return (const void *)k_stage<RECON, RS_LHLLC>;
-    case RS_NONE: return RECON == RECON_DC ? (const void *)k_stage<RECON_DC, RS_NONE> : nullptr;
+    case RS_HLLE: return (const void *)k_stage<RECON, RS_HLLE, MINB>;
+    case RS_HLLC: return (const void *)k_stage<RECON, RS_HLLC, MINB>;
+    case RS_LHLLC: return (const void *)k_stage<RECON, RS_LHLLC, MINB>;
+    case RS_NONE: return RECON == RECON_DC ? (const void *)k_stage<RECON_DC, RS_NONE, MINB> : nullptr;
     default: return nullptr;
   }
 }
 
-const void *stage_kernel(int recon, int rsolver) {
-  if (recon == RECON_PPM) return kernel_for_rs<RECON_PPM>(rsolver);
-  if (recon == RECON_PLM) return kernel_for_rs<RECON_PLM>(rsolver);
-  if (recon == RECON_DC) return kernel_for_rs<RECON_DC>(rsolver);
+template <int MINB>
+static const void *stage_kernel_t(int recon, int rsolver) {
+  if (recon == RECON_PPM) return kernel_for_rs<RECON_PPM, MINB>(rsolver);
+  if (recon == RECON_PLM) return kernel_for_rs<RECON_PLM, MINB>(rsolver);
+  if (recon == RECON_DC) return kernel_for_rs<RECON_DC, MINB>(rsolver);
   return nullptr;
 }
 
-cudaError_t stage_occupancy(int recon, int rsolver, int threads, size_t smem, int *blocks) {
-  const void *k = stage_kernel(recon, rsolver);
+const void *stage_kernel(int recon, int rsolver, int reg_cap) {
+  return reg_cap ? stage_kernel_t<3>(recon, rsolver) : stage_kernel_t<1>(recon, rsolver);
+}
+
+cudaError_t stage_occupancy(int recon, int rsolver, int threads, size_t smem, int reg_cap, int *blocks) {
+  const void *k = stage_kernel(recon, rsolver, reg_cap);
   if (!k) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -678,8 +685,8 @@ cudaError_t stage_occupancy(int recon, int rsolver, int threads, size_t smem, in
 }
 
 cudaError_t launch_stage(const StageArgs &a, int recon, int rsolver, int grid, int threads,
-                         size_t smem, bool cooperative, cudaStream_t s) {
-  const void *k = stage_kernel(recon, rsolver);
+                         size_t smem, bool cooperative, int reg_cap, cudaStream_t s) {
+  const void *k = stage_kernel(recon, rsolver, reg_cap);
   if (!k) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);

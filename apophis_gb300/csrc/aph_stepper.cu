@@ -243,8 +243,8 @@ aph_status configure(aph_stepper s) {
   for (int rc : recons) {
     int k = 0;
     cudaError_t e = s->params.exact
-                        ? aph_exact::stage_occupancy(rc, s->params.rsolver, threads, smem, &k)
-                        : aph_fast::stage_occupancy(rc, s->params.rsolver, threads, smem, &k);
+                        ? aph_exact::stage_occupancy(rc, s->params.rsolver, threads, smem, s->cfg.reg_cap, &k)
+                        : aph_fast::stage_occupancy(rc, s->params.rsolver, threads, smem, s->cfg.reg_cap, &k);
     if (e != cudaSuccess) return cuda_fail(e, "stage occupancy");
     per_sm = std::min(per_sm, k);
   }
@@ -312,9 +312,9 @@ cudaError_t launch_one(aph_stepper s, const StageArgs &a, int recon, cudaStream_
   if (e != cudaSuccess) return e;
   if (s->params.exact)
     return aph_exact::launch_stage(a, recon, s->params.rsolver, s->grid, s->cfg.threads, s->smem,
-                                   s->cooperative, st);
+                                   s->cooperative, s->cfg.reg_cap, st);
   return aph_fast::launch_stage(a, recon, s->params.rsolver, s->grid, s->cfg.threads, s->smem,
-                                s->cooperative, st);
+                                s->cooperative, s->cfg.reg_cap, st);
 }
 
 // Enqueue one full RK step (all stages + dt policy).
@@ -601,6 +601,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   }
   s->cfg.schedule = 0;
   s->cfg.use_graph = 1;
+  s->cfg.reg_cap = 0;
   cudaError_t e = cudaSuccess;
   auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
   ck(cudaMalloc(&s->d_u1, sizeof(double) * 5 * cells));
@@ -779,6 +780,7 @@ aph_status aph_stepper_set_config(aph_stepper s, const aph_stepper_config *cfg) 
     return fail(APH_ERR_INVALID, "threads must be a multiple of 32 in 64..1024");
   if (cfg->threads > 256) return fail(APH_ERR_UNSUPPORTED, "stage kernel is built for <= 256 threads");
   if (cfg->schedule < 0 || cfg->schedule > 2) return fail(APH_ERR_INVALID, "schedule not in 0..2");
+  if (cfg->reg_cap < 0 || cfg->reg_cap > 1) return fail(APH_ERR_INVALID, "reg_cap not in 0..1");
   int seen = 0;
   for (int d = 0; d < s->dev.ndim; ++d) {
     if (cfg->order[d] < 1 || cfg->order[d] > s->dev.ndim) return fail(APH_ERR_INVALID, "bad sweep order");
@@ -821,9 +823,9 @@ aph_status aph_stepper_profile(aph_stepper s, int nsteps, double *stage_ms, void
       if (e == cudaSuccess) e = cudaEventRecord(ev[2 * (k * ns + i)], st);
       if (e == cudaSuccess)
         e = s->params.exact ? aph_exact::launch_stage(a, recon, s->params.rsolver, s->grid, s->cfg.threads,
-                                                      s->smem, s->cooperative, st)
+                                                      s->smem, s->cooperative, s->cfg.reg_cap, st)
                             : aph_fast::launch_stage(a, recon, s->params.rsolver, s->grid, s->cfg.threads,
-                                                     s->smem, s->cooperative, st);
+                                                     s->smem, s->cooperative, s->cfg.reg_cap, st);
       if (e == cudaSuccess) e = cudaEventRecord(ev[2 * (k * ns + i) + 1], st);
     }
     if (e == cudaSuccess) e = enqueue_policy(s, false, st);
@@ -928,6 +930,43 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
     if (per < best_t) {
       best_t = per;
       best_c = c;
+    }
+  }
+  // second round: the register-capped kernel (three 256-thread CTAs per SM) with the best
+  // schedule and order, over the line counts
+  {
+    const aph_stepper_config b0 = best_c;
+    std::vector<aph_stepper_config> more;
+    for (int threads : {128, 256})
+      for (int lines : {0, 1, 2, 3}) {
+        aph_stepper_config c = b0;
+        c.reg_cap = 1;
+        c.threads = threads;
+        for (int d = 0; d < 3; ++d) {
+          const int n = s->dev.max_nx[d];
+          const int auto_l = (n + 2 >= threads) ? 1 : std::max(1, threads / (n + 2));
+          c.lines[d] = lines == 0 ? auto_l : lines == 1 ? 2 * auto_l : lines == 2 ? std::max(1, (7 * auto_l) / 3)
+                                                                                  : std::max(1, (5 * auto_l) / 3);
+        }
+        more.push_back(c);
+      }
+    for (const aph_stepper_config &c : more) {
+      if (aph_stepper_set_config(s, &c) != APH_OK) continue;
+      restore();
+      if (aph_stepper_step(s, 1, 0) != APH_OK) continue;
+      cudaEventRecord(e0, 0);
+      if (aph_stepper_step(s, trial_steps, 0) != APH_OK) continue;
+      cudaEventRecord(e1, 0);
+      cudaEventSynchronize(e1);
+      StepCtl c2;
+      if (read_ctl(s, &c2) != APH_OK) break;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      const double per = ms / trial_steps;
+      if (per < best_t) {
+        best_t = per;
+        best_c = c;
+      }
     }
   }
   cudaEventDestroy(e0);

@@ -227,6 +227,8 @@ typedef struct aph_stepper_config {
   int order[3];     /* sweep order (1-based directions); x, y, z in exact mode */
   int schedule;     /* 0 strided, 1 contiguous ranges, 2 dynamic work counter */
   int use_graph;    /* 1: replay the captured step graph */
+  int reg_cap;      /* 1: the stage kernel built for three 256-thread CTAs per SM (about 80
+                       registers per thread); 0: registers as needed (two CTAs) */
 } aph_stepper_config;
 
 /* Allocate the stepper's scratch, run the initial FillDerived + EstimateTimestep

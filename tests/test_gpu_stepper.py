@@ -82,7 +82,8 @@ def test_stepper_configs_agree(cuda):
     ref = None
     for cfgd in [dict(threads=256, schedule=0, lines=[0, 0, 0]),
                  dict(threads=128, schedule=1, lines=[3, 5, 2]),
-                 dict(threads=256, schedule=2, lines=[1, 1, 1])]:
+                 dict(threads=256, schedule=2, lines=[1, 1, 1]),
+                 dict(threads=256, schedule=2, lines=[2, 3, 1], reg_cap=1)]:
         st = Stepper(cfg, cons, exact=True)
         c = st.config
         c.update(cfgd)
