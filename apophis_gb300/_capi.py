@@ -124,6 +124,9 @@ SIGNATURES = {
                             ctypes.c_void_p], ctypes.c_int),
     "aph_hydro_history": ([ctypes.c_void_p, _dp, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_history": ([ctypes.c_void_p, _dp, ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_set_clock": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                               ctypes.c_void_p], ctypes.c_int),
+    "aph_diag_barrier_timeout": ([ctypes.c_double, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_member_status": ([ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int),
                                    ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_get_config": ([ctypes.c_void_p, ctypes.POINTER(aph_stepper_config)],

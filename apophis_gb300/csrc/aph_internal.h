@@ -75,6 +75,7 @@ struct StepCtl {
   unsigned long long min_bits;  // dt reduction (bit pattern of the positive minimum)
   int ncycle;
   int error;                    // aph_status of a device-side failure (barrier timeout)
+  int nonfinite;                // set when an update produced a NaN or an infinity
   unsigned int bar_count, bar_gen;
   unsigned int work[8];         // dynamic work counters, one per phase
 };
@@ -147,6 +148,8 @@ APH_DECLARE_LAUNCHERS(aph_exact)
                            cudaStream_t s);                                                    \
   cudaError_t stage_occupancy(int recon, int rsolver, int threads, size_t smem, int reg_cap,   \
                               int *blocks);                                                    \
+  cudaError_t launch_barrier_probe(aph::StepCtl *ctl, unsigned long long timeout_ns,          \
+                                   cudaStream_t s);                                            \
   }
 APH_DECLARE_STAGE(aph_fast)
 APH_DECLARE_STAGE(aph_exact)

@@ -38,7 +38,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // Grid-wide barrier.  Every CTA of the launch is resident (the grid is sized from the
 // occupancy calculator, and launched cooperatively when possible); a wait that outlasts
 // timeout_ns records APH_ERR_TIMEOUT and the CTA leaves, so the launch always ends.
-__device__ __noinline__ bool grid_barrier(StepCtl *ctl, unsigned long long timeout_ns) {
+__device__ __noinline__ bool grid_barrier(StepCtl *ctl, unsigned long long timeout_ns,
+                                          unsigned int expected) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -48,7 +49,7 @@ __device__ __noinline__ bool grid_barrier(StepCtl *ctl, unsigned long long timeo
     const unsigned int gen = *vgen;
     __threadfence();
     const unsigned int arrived = atomicAdd(&ctl->bar_count, 1u) + 1u;
-    if (arrived == gridDim.x) {
+    if (arrived == expected) {
       atomicExch(&ctl->bar_count, 0u);
       __threadfence();
       atomicAdd(&ctl->bar_gen, 1u);
@@ -444,8 +445,13 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
           }
           u[IEN] += de * rho * beta_dt;
         }
+        bool bad = false;
 #pragma unroll
-        for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + cell] = u[v];
+        for (int v = 0; v < NHYDRO; ++v) {
+          B.u0[v * nc + cell] = u[v];
+          bad |= ((__double_as_longlong(u[v]) >> 52) & 0x7ff) == 0x7ff;  // NaN or inf
+        }
+        if (bad) a.ctl->nonfinite = 1;
         if (a.last) {  // EstimateTimestep on the floored new state
           double w[NHYDRO], gcc, gce;
           const bool fl = cons_to_prim_cell(u, w, gcc, gce, gc.gm1, a.p.dfloor, a.p.pfloor);
@@ -519,8 +525,13 @@ __device__ void amr_update(const StageArgs &a, const Sched &sched, unsigned int 
       de += a.grav[1] * B.prim[IV2 * nc + c];
       u[IEN] += de * rho * beta_dt;
     }
+    bool bad = false;
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + c] = u[v];
+    for (int v = 0; v < NHYDRO; ++v) {
+      B.u0[v * nc + c] = u[v];
+      bad |= ((__double_as_longlong(u[v]) >> 52) & 0x7ff) == 0x7ff;  // NaN or inf
+    }
+    if (bad) a.ctl->nonfinite = 1;
     if (a.last) {
       double wv[NHYDRO], gcc, gce;
       cons_to_prim_cell(u, wv, gcc, gce, p.gm1, p.dfloor, p.pfloor);
@@ -558,7 +569,7 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
   if (!a.init)
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < p.nblocks; b += gridDim.x * blockDim.x)
       a.block_flags[b] = 0;
-  if (!grid_barrier(a.ctl, a.timeout_ns)) return;
+  if (!grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
 
   // phase 1: ConsToPrim (in init mode only the dt estimate, nothing is written)
   for (int it = sched.first(ctr + 1, a.ncell_items); it < a.ncell_items;
@@ -608,7 +619,7 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
     if (threadIdx.x == 0 && dtmin != ~0ULL) atomicMin(&a.ctl->min_bits, dtmin);
     return;
   }
-  if (!grid_barrier(a.ctl, a.timeout_ns)) return;
+  if (!grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
 
   // phases 2..: one pass per direction
   for (int pi = 0; pi < p.ndim; ++pi) {
@@ -634,12 +645,12 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
       else
         pass_item<3, RECON, RS>(a, B, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin);
     }
-    if (!last_pass && !grid_barrier(a.ctl, a.timeout_ns)) return;
+    if (!last_pass && !grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
   }
   if (a.cf) {
-    if (!grid_barrier(a.ctl, a.timeout_ns)) return;
+    if (!grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
     amr_correct(a, sched, ctr + 6);
-    if (!grid_barrier(a.ctl, a.timeout_ns)) return;
+    if (!grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
     amr_update(a, sched, ctr + 7, dtmin);
   }
   if (a.last) {
@@ -648,7 +659,18 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
   }
 }
 
+// Failure-path probe: one CTA waits at a grid barrier for one more CTA than the launch has,
+// so the wait runs out after timeout_ns and records APH_ERR_TIMEOUT in ctl.
+__global__ void k_barrier_probe(StepCtl *ctl, unsigned long long timeout_ns) {
+  grid_barrier(ctl, timeout_ns, gridDim.x + 1);
+}
+
 // ---- host side ---------------------------------------------------------------------------
+cudaError_t launch_barrier_probe(StepCtl *ctl, unsigned long long timeout_ns, cudaStream_t s) {
+  k_barrier_probe<<<1, 32, 0, s>>>(ctl, timeout_ns);
+  return cudaGetLastError();
+}
+
 size_t stage_smem_bytes(int recon, int n, int T) {
   return pass_smem_doubles(recon, n, T, 7) * sizeof(double);
 }

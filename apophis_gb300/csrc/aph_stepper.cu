@@ -28,6 +28,7 @@ __global__ void k_ctl_init(StepCtl *c, double tlim, double dt_fixed) {
   c->min_bits = ~0ULL;
   c->ncycle = 0;
   c->error = 0;
+  c->nonfinite = 0;
   c->bar_count = 0;
   c->bar_gen = 0;
   for (int i = 0; i < 8; ++i) c->work[i] = 0;
@@ -374,6 +375,7 @@ aph_status read_ctl(aph_stepper s, StepCtl *out) {
   cudaError_t e = cudaMemcpy(out, s->d_ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "read stepper state");
   if (out->error) return fail(out->error, "device-side failure in the stage kernel (status %d)", out->error);
+  if (out->nonfinite) return fail(APH_ERR_STATE, "an update produced a NaN or an infinity");
   return APH_OK;
 }
 
@@ -765,6 +767,24 @@ aph_status aph_stepper_history(aph_stepper s, double out[2], void *stream) {
   return e == cudaSuccess ? APH_OK : cuda_fail(e, "stepper history");
 }
 
+aph_status aph_stepper_set_clock(aph_stepper s, double time, double dt, int ncycle, void *stream) {
+  clear_error();
+  if (!s) return fail(APH_ERR_INVALID, "stepper is NULL");
+  if (s->d_members) return fail(APH_ERR_UNSUPPORTED, "an ensemble keeps one clock per member");
+  if (!(dt >= 0.0) || ncycle < 0) return fail(APH_ERR_INVALID, "dt and ncycle must be >= 0");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaStreamSynchronize(st);
+  StepCtl c;
+  if (e == cudaSuccess) e = cudaMemcpy(&c, s->d_ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "set clock");
+  c.time = time;
+  c.dt = dt;
+  c.ncycle = ncycle;
+  c.min_bits = ~0ULL;
+  e = cudaMemcpy(s->d_ctl, &c, sizeof(StepCtl), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "set clock");
+}
+
 aph_status aph_stepper_get_config(aph_stepper s, aph_stepper_config *cfg) {
   clear_error();
   if (!s || !cfg) return fail(APH_ERR_INVALID, "NULL argument");
@@ -978,6 +998,25 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
   if (best) aph_stepper_get_config(s, best);
   if (best_ms) *best_ms = best_t;
   return st;
+}
+
+aph_status aph_diag_barrier_timeout(double timeout_s, void *stream) {
+  clear_error();
+  if (!(timeout_s > 0.0) || timeout_s > 10.0) return fail(APH_ERR_INVALID, "timeout must be in (0, 10] s");
+  StepCtl *ctl = nullptr;
+  cudaError_t e = cudaMalloc(&ctl, sizeof(StepCtl));
+  if (e != cudaSuccess) return cuda_fail(e, "barrier probe");
+  cudaStream_t st = (cudaStream_t)stream;
+  k_ctl_init<<<1, 1, 0, st>>>(ctl, DBL_MAX, 0.0);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = aph_fast::launch_barrier_probe(ctl, (unsigned long long)(timeout_s * 1e9), st);
+  StepCtl c;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemcpy(&c, ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost);
+  cudaFree(ctl);
+  if (e != cudaSuccess) return cuda_fail(e, "barrier probe");
+  if (c.error) return fail(c.error, "the probe's grid barrier gave up after %.3f s", timeout_s);
+  return APH_OK;
 }
 
 }  // extern "C"

@@ -73,6 +73,32 @@ class Stepper:
                    ctypes.byref(n), stream_handle(stream))
         return {"time": t.value, "dt": dt.value, "ncycle": n.value}
 
+    def save(self, base):
+        """Checkpoint: the state as an output dump (output.write_dump) with the clock."""
+        from . import output
+        st = self.status()
+        output.write_dump(base, self.cfg, self.state(), st["time"], st["ncycle"])
+        import json
+        meta = json.load(open(base + ".json"))
+        meta["NextDt"] = st["dt"]
+        meta["Exact"] = int(self.exact)
+        with open(base + ".json", "w") as f:
+            json.dump(meta, f, indent=1)
+
+    @classmethod
+    def restore(cls, base, cfg: MeshConfig, exact=None, tlim=None):
+        """Resume from save(): the dump's interiors (ghosts are refilled by the first stage)
+        and its clock."""
+        from . import output
+        d = output.Dump(base)
+        cons = np.zeros(cfg.pack_shape(5))
+        sk, sj, si = cfg.interior
+        cons[:, :, sk, sj, si] = d.Get("cons", flatten=False)
+        st = cls(cfg, cons, exact=bool(d.meta.get("Exact", 0)) if exact is None else exact, tlim=tlim)
+        _capi.call("aph_stepper_set_clock", st.h, float(d.Time), float(d.meta["NextDt"]),
+                   int(d.NCycle), stream_handle())
+        return st
+
     def history(self, stream=None):
         """GlobalQuantHst of the state: {"total_mass", "total_energy"}."""
         out = (ctypes.c_double * 2)()

@@ -246,6 +246,10 @@ aph_status aph_stepper_status(aph_stepper stepper, double *time, double *dt, int
  * member time, the largest next dt and the largest cycle count. */
 aph_status aph_stepper_member_status(aph_stepper stepper, double *time, double *dt, int *ncycle,
                                      void *stream);
+/* Resume: set the clock (time, dt of the next step, cycle count) of a stepper created from a
+ * saved state (no ensemble). */
+aph_status aph_stepper_set_clock(aph_stepper stepper, double time, double dt, int ncycle,
+                                 void *stream);
 /* The history sums of the stepper's state (as aph_hydro_history, over all blocks). */
 aph_status aph_stepper_history(aph_stepper stepper, double out[2], void *stream);
 aph_status aph_stepper_get_config(aph_stepper stepper, aph_stepper_config *cfg);
@@ -257,6 +261,13 @@ aph_status aph_stepper_profile(aph_stepper stepper, int nsteps, double *stage_ms
  * of the state (the state and clock are restored) and keep the fastest. */
 aph_status aph_stepper_autotune(aph_stepper stepper, int trial_steps, aph_stepper_config *best,
                                 double *best_ms);
+
+/* Failure-path probe (no counterpart in the reference): a one-CTA launch whose grid barrier
+ * waits for a CTA that does not exist.  The wait gives up after timeout_s (<= 10) and the call
+ * returns APH_ERR_TIMEOUT, the status every persistent stage launch reports when a barrier
+ * runs out; the context stays usable.  Stepper status calls also return APH_ERR_STATE once an
+ * update has produced a NaN or an infinity. */
+aph_status aph_diag_barrier_timeout(double timeout_s, void *stream);
 
 /* ---- adjoint of the step --------------------------------------------------------------
  * Hand-written reverse mode of the full fixed-dt step: ConsToPrim, the PPM, PLM or

@@ -143,3 +143,16 @@ def test_stepper_rejects_bad_ensembles():
                dict(gm1=[0.4, -1.0])):
         st, _keep = make(**kw)
         assert st == 1, (kw, st, _capi.load().aph_last_error())  # APH_ERR_INVALID
+
+
+def test_bad_ghost_width_and_floors_rejected():
+    """Validation before any device work: PPM with 2 ghost cells (hydro.cpp:72-75)."""
+    import ctypes
+    lib = _capi.load()
+    p = _capi.aph_hydro_params(2, 2, 5, 3, 3, 0.4, 1e-10, 1e-10, 0.3, 0)  # ppm, ng 2
+    blk = (_capi.aph_block * 1)()
+    blk[0].cons = 4096
+    blk[0].nx[:] = [8, 8, 1]
+    blk[0].dx[:] = [0.1, 0.1, 1.0]
+    h = ctypes.c_void_p()
+    assert lib.aph_pack_create(ctypes.byref(p), blk, 1, ctypes.byref(h)) == 1
