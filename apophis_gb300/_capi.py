@@ -56,13 +56,13 @@ class aph_stepper_config(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
                 ("lines", ctypes.c_int * 3), ("order", ctypes.c_int * 3),
                 ("schedule", ctypes.c_int), ("use_graph", ctypes.c_int),
-                ("reg_cap", ctypes.c_int)]
+                ("reg_cap", ctypes.c_int), ("tma", ctypes.c_int)]
 
     def to_dict(self):
         return {"threads": self.threads, "ctas_per_sm": self.ctas_per_sm,
                 "lines": list(self.lines), "order": list(self.order),
                 "schedule": self.schedule, "use_graph": self.use_graph,
-                "reg_cap": self.reg_cap}
+                "reg_cap": self.reg_cap, "tma": self.tma}
 
     @classmethod
     def from_dict(cls, d):
@@ -74,6 +74,7 @@ class aph_stepper_config(ctypes.Structure):
         c.schedule = d["schedule"]
         c.use_graph = d.get("use_graph", 1)
         c.reg_cap = d.get("reg_cap", 0)
+        c.tma = d.get("tma", 0)
         return c
 
 

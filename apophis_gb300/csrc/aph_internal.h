@@ -105,6 +105,8 @@ struct StageArgs {
   int bflux_stride;             // doubles per face of bflux (max transverse cells * 5)
   int cf;                       // refined meshes with coarse-fine faces: correction phases
   MemberCtl *members;           // ensembles (NULL: one problem, clock in ctl)
+  const void *tmaps;            // TMA: three tensor maps (x, y, z windows) over prim, or NULL
+  int ext[3];                   // TMA: entire extents ni, nj, nk of every block
   int T[3];
   int order[3];                 // sweep order (1-based directions)
   double gam0, gam1, beta;
@@ -142,6 +144,7 @@ APH_DECLARE_LAUNCHERS(aph_exact)
 #define APH_DECLARE_STAGE(NS)                                                                  \
   namespace NS {                                                                               \
   size_t stage_smem_bytes(int recon, int n, int T);                                            \
+  size_t stage_smem_bytes_tma(int recon, int n, int T, int L);                                 \
   const void *stage_kernel(int recon, int rsolver);                                            \
   cudaError_t launch_stage(const aph::StageArgs &a, int recon, int rsolver, int grid,          \
                            int threads, size_t smem, bool cooperative, int reg_cap,            \

@@ -72,6 +72,62 @@ __device__ __noinline__ bool grid_barrier(StepCtl *ctl, unsigned long long timeo
   return s_ok != 0;
 }
 
+// ---- TMA staging of a pass item's window ----------------------------------------------------
+// With a.tmaps set, the prim window of a constant-gamma item comes in as one 5D tensor copy
+// (cp.async.bulk.tensor) of the whole line extent of its T lines, all five variables, from
+// the pack's prim viewed as [block][var][k][j][i]; an mbarrier with its transaction count
+// signals completion and every thread waits on it with a time bound.
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(bar), "r"(phase)
+      : "memory");
+  return done != 0;
+}
+
+// Wait for the copy of this phase; after timeout_ns the wait records APH_ERR_TIMEOUT and
+// keeps waiting for the copy in flight for up to another timeout_ns before giving up.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase, StepCtl *ctl,
+                                                  unsigned long long timeout_ns) {
+  if (mbar_try_wait(bar, phase)) return true;
+  const unsigned long long t0 = global_ns();
+  bool late = false;
+  while (!mbar_try_wait(bar, phase)) {
+    const unsigned long long dt = global_ns() - t0;
+    if (!late && dt > timeout_ns) {
+      atomicCAS(&ctl->error, 0, 4 /* APH_ERR_TIMEOUT */);
+      late = true;
+    }
+    if (dt > 2 * timeout_ns) return false;
+  }
+  return !late;
+}
+
+__device__ __forceinline__ void tma_load_5d(unsigned dst, const void *tmap, unsigned bar, int c0,
+                                            int c1, int c2, int c3, int c4) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+      "l"((unsigned long long)tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+      : "memory");
+}
+
 // Work distribution of a phase with n items.
 struct Sched {
   int mode;
@@ -253,11 +309,18 @@ __host__ __device__ constexpr size_t pass_smem_doubles(int recon, int n, int T, 
              : (size_t)V * T * ((n + 2 * (recon == RECON_PLM ? 2 : 1)) + 2 * (n + 2));
 }
 
-// One pass item: lines l0..l0+nl-1 of block B along DIR.
+// Doubles between the window region and the TMA staging area: the window is padded to a
+// multiple of 16 doubles so that the staging area starts 128-byte aligned.
+__host__ __device__ constexpr size_t tma_stage_offset(int recon, int n, int T) {
+  return ((size_t)7 * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1)) + 15) / 16 * 16;
+}
+
+// One pass item: lines l0..l0+nl-1 of block B along DIR.  b: the block's index in the pack;
+// tma_phase: the parity of the CTA's next mbarrier phase (TMA items flip it).
 template <int DIR, int RECON, int RS>
-__device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl, int T,
+__device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0, int nl, int T,
                           bool constg, bool first_pass, bool last_pass, double *sm,
-                          unsigned long long &dtmin) {
+                          unsigned long long &dtmin, unsigned mbar, unsigned &tma_phase) {
   constexpr int G = Halo<RECON>::G;
   const int n = B.nx[DIR - 1];
   const int V = constg ? 5 : 7;
@@ -276,7 +339,48 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int l0, int nl
   auto w_at = [&](int v, int t, int c) -> double & { return W[((size_t)v * T + t) * NW + c + G]; };
 
   // A: load the window of prim (and gamma) along each line
-  {
+  if (a.tmaps && constg) {
+    // one tensor copy of the T lines' whole extent into the staging area, then the window
+    // cells -G..n+G-1 into W (the staging layout is [v][t][i] along x, [v][w][t] along y, z)
+    // 128-byte aligned staging area after the window region (the size reserves the slack)
+    double *stg = (double *)(((unsigned long long)(sm + tma_stage_offset(RECON, n, T)) + 127ULL) & ~127ULL);
+    const int L = a.ext[DIR - 1];
+    const int ng = a.p.ng;
+    // order every thread's earlier generic accesses of this shared memory before the copy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    // the item's lines lie in one plane of the block, or in two consecutive planes: one box
+    // of T lines at each (lines of a box beyond the item are loaded and not used)
+    const int per_plane = DIR == 1 ? B.nx[1] : B.nx[0];
+    const int lp = l0 % per_plane, plane = l0 / per_plane;
+    const int T1 = min(nl, per_plane - lp);
+    const size_t box = (size_t)NHYDRO * T * L;
+    if (tid == 0) {
+      const unsigned bytes = (unsigned)((nl > T1 ? 2 : 1) * box * sizeof(double));
+      mbar_expect_tx(mbar, bytes);
+      const char *maps = (const char *)a.tmaps;
+      const int sj = a.p.ndim >= 2 ? ng : 0, sk = a.p.ndim >= 3 ? ng : 0;
+      for (int part = 0; part < (nl > T1 ? 2 : 1); ++part) {
+        const int pos = part == 0 ? lp : 0, pl = plane + part;
+        const unsigned dst = smem_addr(stg + part * box);
+        if (DIR == 1) tma_load_5d(dst, maps, mbar, 0, pos + sj, pl + sk, 0, b);
+        else if (DIR == 2) tma_load_5d(dst, maps + 128, mbar, pos + ng, 0, pl + sk, 0, b);
+        else tma_load_5d(dst, maps + 256, mbar, pos + ng, pl + sj, 0, 0, b);
+      }
+    }
+    mbar_wait_bounded(mbar, tma_phase, a.ctl, a.timeout_ns);
+    tma_phase ^= 1u;
+    for (int it = tid; it < NHYDRO * nl * NW; it += nth) {
+      const int v = it / (nl * NW);
+      const int r = it - v * nl * NW;
+      const int t = r / NW, w = r - t * NW;
+      const int cell = w - G + ng;  // position along the line's whole extent
+      const double *src = t < T1 ? stg : stg + box;
+      const int tt = t < T1 ? t : t - T1;
+      W[((size_t)v * T + t) * NW + w] = DIR == 1 ? src[((size_t)v * T + tt) * L + cell]
+                                                 : src[((size_t)v * L + cell) * T + tt];
+    }
+  } else {
     const int per = nl * NW;
     for (int it = tid; it < V * per; it += nth) {
       const int v = it / per;
@@ -545,7 +649,14 @@ __device__ void amr_update(const StageArgs &a, const Sched &sched, unsigned int 
 // wants; 3: capped near 80 per thread for 256-thread CTAs, trading a few spills for occupancy).
 template <int RECON, int RS, int MINB>
 __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(128) double sm[];
+  __shared__ __align__(8) unsigned long long s_mbar;
+  const unsigned mbar = smem_addr(&s_mbar);
+  unsigned tma_phase = 0;
+  if (a.tmaps && threadIdx.x == 0) {
+    mbar_init(mbar);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
   const PackDev &p = a.p;
   const Sched sched{a.schedule};
   unsigned long long dtmin = ~0ULL;
@@ -639,11 +750,14 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
       const bool constg = a.block_flags[w.x] == 0;
 #endif
       if (dir == 1)
-        pass_item<1, RECON, RS>(a, B, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin);
+        pass_item<1, RECON, RS>(a, B, w.x, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin, mbar,
+                                tma_phase);
       else if (dir == 2)
-        pass_item<2, RECON, RS>(a, B, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin);
+        pass_item<2, RECON, RS>(a, B, w.x, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin, mbar,
+                                tma_phase);
       else
-        pass_item<3, RECON, RS>(a, B, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin);
+        pass_item<3, RECON, RS>(a, B, w.x, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin, mbar,
+                                tma_phase);
     }
     if (!last_pass && !grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
   }
@@ -673,6 +787,15 @@ cudaError_t launch_barrier_probe(StepCtl *ctl, unsigned long long timeout_ns, cu
 
 size_t stage_smem_bytes(int recon, int n, int T) {
   return pass_smem_doubles(recon, n, T, 7) * sizeof(double);
+}
+
+// With TMA staging: the window region padded to 128 bytes, then the larger of the remaining
+// pass regions and the staging area (5 variables x T lines x the line's entire extent L).
+size_t stage_smem_bytes_tma(int recon, int n, int T, int L) {
+  const size_t rest = pass_smem_doubles(recon, n, T, 7) -
+                      (size_t)7 * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1));
+  const size_t stage = (size_t)2 * NHYDRO * T * L;  // two boxes for items that cross a plane
+  return (tma_stage_offset(recon, n, T) + 16 + (rest > stage ? rest : stage)) * sizeof(double);
 }
 
 template <int RECON, int MINB>

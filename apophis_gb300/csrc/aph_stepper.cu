@@ -10,6 +10,9 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "../../include/aph_hydro.h"
 #include "aph_capi_internal.h"
 #include "aph_internal.h"
@@ -174,6 +177,7 @@ struct aph_stepper_s {
   int nmembers = 0;
   double *d_hist = nullptr;        // history partial sums (allocated on first use)
   size_t hist_len = 0;
+  void *d_tmaps = nullptr;         // TMA: tensor maps of the x, y, z windows (3 x 128 bytes)
 };
 
 namespace {
@@ -196,6 +200,67 @@ void destroy_graph(aph_stepper s) {
   s->graph = nullptr;
 }
 
+// TMA staging of pass windows (cfg.tma): every block of the same size, laid out back to back
+// in prim as [block][var][k][j][i]; TMA's rules: 16-byte strides (ni even), each box side
+// <= 256, the innermost box side a multiple of 16 bytes (T even across y and z) starting on
+// a 16-byte boundary (nghost even, item starts even); an item spans at most two planes of
+// lines (T <= the lines of a plane).  Returns nullptr or the reason.
+const char *tma_unsupported(aph_stepper s, const int T[3]) {
+  const PackDev &p = s->dev;
+  const StepBlock &B0 = s->hblocks[0];
+  for (const StepBlock &B : s->hblocks)
+    for (int d = 0; d < 3; ++d)
+      if (B.nx[d] != B0.nx[d]) return "blocks of different sizes";
+  if (B0.ni % 2) return "an odd row length";
+  if (p.ng % 2) return "an odd ghost width";
+  const int ext[3] = {B0.ni, B0.nj, B0.nk};
+  for (int d = 0; d < p.ndim; ++d) {
+    if (ext[d] > 256 || T[d] > 256) return "a window side above 256";
+    if (d == 0 && T[0] > B0.nx[1]) return "x items longer than a plane of lines";
+    if (d > 0 && (T[d] % 2 || B0.nx[0] % 2 || T[d] > B0.nx[0]))
+      return "y/z items of an odd line count, odd planes or items longer than a plane";
+  }
+  return nullptr;
+}
+
+aph_status encode_tmaps(aph_stepper s) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+      return fail(APH_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+    encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  const StepBlock &B0 = s->hblocks[0];
+  const PackDev &p = s->dev;
+  const cuuint64_t dims[5] = {(cuuint64_t)B0.ni, (cuuint64_t)B0.nj, (cuuint64_t)B0.nk, 5,
+                              (cuuint64_t)p.nblocks};
+  const cuuint64_t strides[4] = {(cuuint64_t)B0.ni * 8, (cuuint64_t)B0.ni * B0.nj * 8,
+                                 (cuuint64_t)B0.ncell * 8, (cuuint64_t)B0.ncell * 5 * 8};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  CUtensorMap maps[3];
+  std::memset(maps, 0, sizeof(maps));
+  for (int d = 0; d < 3; ++d) {
+    cuuint32_t box[5] = {1, 1, 1, 5, 1};
+    const int T = std::max(1, s->T[d]);
+    if (d == 0) { box[0] = B0.ni; box[1] = T; }
+    else if (d == 1) { box[0] = T; box[1] = B0.nj; }
+    else { box[0] = T; box[2] = B0.nk; }
+    if (d >= p.ndim) continue;
+    CUresult r = encode(&maps[d], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, (void *)s->d_prim, dims, strides, box,
+                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(APH_ERR_UNSUPPORTED, "tensor map encoding failed (%d)", (int)r);
+  }
+  cudaError_t e = cudaSuccess;
+  if (!s->d_tmaps) e = cudaMalloc(&s->d_tmaps, sizeof(maps));
+  if (e == cudaSuccess) e = cudaMemcpy(s->d_tmaps, maps, sizeof(maps), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "tensor maps");
+}
+
 // Build work lists, shared-memory size and grid for the current configuration.
 aph_status configure(aph_stepper s) {
   destroy_graph(s);
@@ -214,8 +279,11 @@ aph_status configure(aph_stepper s) {
     }
     T = std::min(T, ntr_max);
     s->T[d] = T;
-    const size_t need = s->params.exact ? aph_exact::stage_smem_bytes(recon, n, T)
-                                        : aph_fast::stage_smem_bytes(recon, n, T);
+    const int ext = d == 0 ? s->hblocks[0].ni : d == 1 ? s->hblocks[0].nj : s->hblocks[0].nk;
+    const size_t need = s->cfg.tma ? (s->params.exact ? aph_exact::stage_smem_bytes_tma(recon, n, T, ext)
+                                                      : aph_fast::stage_smem_bytes_tma(recon, n, T, ext))
+                                   : (s->params.exact ? aph_exact::stage_smem_bytes(recon, n, T)
+                                                      : aph_fast::stage_smem_bytes(recon, n, T));
     smem = std::max(smem, need);
     std::vector<int2> items;
     // schedule order: largest blocks first (longest-processing-time) so that the tail of a
@@ -235,6 +303,11 @@ aph_status configure(aph_stepper s) {
   }
   if (smem > 220 * 1024)
     return fail(APH_ERR_UNSUPPORTED, "stage needs %zu bytes of shared memory; use fewer lines", smem);
+  if (s->cfg.tma) {
+    if (const char *why = tma_unsupported(s, s->T))
+      return fail(APH_ERR_UNSUPPORTED, "TMA windows need other lines per item or blocks: %s", why);
+    if (aph_status st = encode_tmaps(s)) return st;
+  }
   s->smem = smem;
   const int threads = s->cfg.threads;
   // every kernel instance a step launches (vl2's first stage reconstructs donor-cell)
@@ -293,6 +366,10 @@ StageArgs stage_args(aph_stepper s, int stage_idx, const Stage &st, bool last, b
   a.bflux_stride = s->bflux_stride;
   a.cf = s->nfix_items > 0;
   a.members = s->d_members;
+  a.tmaps = s->cfg.tma ? s->d_tmaps : nullptr;
+  a.ext[0] = s->hblocks[0].ni;
+  a.ext[1] = s->hblocks[0].nj;
+  a.ext[2] = s->hblocks[0].nk;
   return a;
 }
 
@@ -396,6 +473,7 @@ void free_all(aph_stepper s) {
   cudaFree(s->d_bflux);
   cudaFree(s->d_members);
   cudaFree(s->d_hist);
+  cudaFree(s->d_tmaps);
 }
 
 __global__ void k_set_dt(StepCtl *c, MemberCtl *m, int n, const double *dt) {
@@ -604,6 +682,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   s->cfg.schedule = 0;
   s->cfg.use_graph = 1;
   s->cfg.reg_cap = 0;
+  s->cfg.tma = 0;
   cudaError_t e = cudaSuccess;
   auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
   ck(cudaMalloc(&s->d_u1, sizeof(double) * 5 * cells));
@@ -801,6 +880,7 @@ aph_status aph_stepper_set_config(aph_stepper s, const aph_stepper_config *cfg) 
   if (cfg->threads > 256) return fail(APH_ERR_UNSUPPORTED, "stage kernel is built for <= 256 threads");
   if (cfg->schedule < 0 || cfg->schedule > 2) return fail(APH_ERR_INVALID, "schedule not in 0..2");
   if (cfg->reg_cap < 0 || cfg->reg_cap > 1) return fail(APH_ERR_INVALID, "reg_cap not in 0..1");
+  if (cfg->tma < 0 || cfg->tma > 1) return fail(APH_ERR_INVALID, "tma not in 0..1");
   int seen = 0;
   for (int d = 0; d < s->dev.ndim; ++d) {
     if (cfg->order[d] < 1 || cfg->order[d] > s->dev.ndim) return fail(APH_ERR_INVALID, "bad sweep order");
@@ -968,6 +1048,16 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
           c.lines[d] = lines == 0 ? auto_l : lines == 1 ? 2 * auto_l : lines == 2 ? std::max(1, (7 * auto_l) / 3)
                                                                                   : std::max(1, (5 * auto_l) / 3);
         }
+        more.push_back(c);
+      }
+    // each with TMA-staged windows too, where the lines allow it (even, dividing a plane)
+    const size_t nmore = more.size();
+    for (size_t i = 0; i < nmore; ++i)
+      for (int rc : {0, 1}) {
+        aph_stepper_config c = more[i];
+        c.reg_cap = rc;
+        c.tma = 1;
+        for (int d = 0; d < 3; ++d) c.lines[d] = std::max(2, c.lines[d] - c.lines[d] % 2);
         more.push_back(c);
       }
     for (const aph_stepper_config &c : more) {

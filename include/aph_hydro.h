@@ -229,6 +229,9 @@ typedef struct aph_stepper_config {
   int use_graph;    /* 1: replay the captured step graph */
   int reg_cap;      /* 1: the stage kernel built for three 256-thread CTAs per SM (about 80
                        registers per thread); 0: registers as needed (two CTAs) */
+  int tma;          /* 1: stage each pass item's prim window with one tensor copy (TMA) when
+                       the blocks are equal, rows even, nghost even and the lines per item
+                       even and dividing a plane; 0: plain loads */
 } aph_stepper_config;
 
 /* Allocate the stepper's scratch, run the initial FillDerived + EstimateTimestep

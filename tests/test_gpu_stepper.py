@@ -130,3 +130,29 @@ def test_stepper_autotune_keeps_state(cuda, tmp_path):
     st2 = Stepper(cfg, cons, exact=True)
     rec2 = st2.autotune(trial_steps=1, cache=str(tmp_path / "tune.json"))
     assert rec2["config"] == rec["config"]
+
+
+@pytest.mark.parametrize("make,lines", [
+    (lambda: problems.kh3d(n=16, block=8, ng=4), [2, 2, 2]),
+    (lambda: problems.kh3d(n=16, block=8, ng=4), [4, 4, 4]),
+    (lambda: problems.kh2d(n=64, block=32, ng=4, recon="ppm", rsolver="hllc"), [4, 8, 0]),
+    (lambda: problems.kh2d(n=64, block=32, ng=2, recon="plm", rsolver="hlle"), [2, 2, 0]),
+    # items crossing a plane of lines (two tensor copies)
+    (lambda: problems.kh3d(n=16, block=8, ng=4), [6, 6, 6]),
+    (lambda: problems.kh2d(n=64, block=32, ng=4, recon="ppm", rsolver="hllc"), [6, 6, 0]),
+])
+def test_stepper_tma_windows_match_plain_loads(cuda, make, lines):
+    """TMA-staged windows change only how prim reaches shared memory: bit-identical steps."""
+    cfg, cons = make()
+    outs = []
+    for tma in (0, 1):
+        for reg_cap in (0, 1):
+            st = Stepper(cfg, cons, exact=False)
+            c = st.config
+            c.update(lines=lines, tma=tma, reg_cap=reg_cap, schedule=2)
+            st.set_config(c)
+            st.step(3)
+            outs.append((st.state(), st.status()))
+            st.close()
+    for out, status in outs[1:]:
+        assert np.array_equal(out, outs[0][0]) and status == outs[0][1]
