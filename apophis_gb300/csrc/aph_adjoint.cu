@@ -114,7 +114,7 @@ __device__ __forceinline__ void riemann_pass_vjp(const AdjMember &M, int T, int 
 
 // PLM / donor-cell pass.
 template <int DIR, int RECON, int RS>
-__global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim, const double *mu,
+__global__ void __launch_bounds__(256, 2) k_adj_pass(AdjGeom g, const double *prim, const double *mu,
                                                   double *lam_w, double beta, const double *dt, int T) {
   extern __shared__ double sm[];
   constexpr int G = RECON == RECON_PLM ? 2 : 1;
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(256) k_adj_pass(AdjGeom g, const double *prim,
 __host__ __device__ constexpr size_t ppm_pass_slab(int n, int T) { return (size_t)5 * T * (n + 6); }
 
 template <int DIR, int RS>
-__global__ void __launch_bounds__(256) k_adj_pass_ppm(AdjGeom g, const double *prim, const double *mu,
+__global__ void __launch_bounds__(256, 2) k_adj_pass_ppm(AdjGeom g, const double *prim, const double *mu,
                                                       double *lam_w, double beta, const double *dt, int T) {
   extern __shared__ double sm[];
   constexpr int G = 3;

@@ -247,6 +247,24 @@ __device__ __forceinline__ SoundSpeed sound_speed_d(double rho, double p, double
   return s;
 }
 
+// Adjoint of one side's physical flux  F = (rho vx, rho u vx + p, rho v vx, rho z vx, e vx + p u)
+// with vx = u - b and e = p/gm1 + rho |v|^2 / 2, for the flux adjoint g: adds to gw
+// (rho, u, v, z, p) and returns the adjoint of vx (the b-dependence is the caller's).
+__device__ __forceinline__ double side_flux_vjp(const double *w, double vx, double e, double igm1,
+                                                const double *g, double *gw) {
+  const double rho = w[IDN], u = w[IV1], v = w[IV2], z = w[IV3], p = w[IPR];
+  const double A = g[0] + g[1] * u + g[2] * v + g[3] * z;  // shared by d/drho and d/dvx
+  const double rvx = rho * vx;
+  const double ge = g[4] * vx;                               // adjoint of e
+  const double rge = rho * ge;
+  gw[IDN] += A * vx + ge * 0.5 * (u * u + v * v + z * z);
+  gw[IV1] += g[1] * rvx + g[4] * p + rge * u;
+  gw[IV2] += g[2] * rvx + rge * v;
+  gw[IV3] += g[3] * rvx + rge * z;
+  gw[IPR] += g[1] + g[4] * u + ge * igm1;
+  return rho * A + g[4] * e;
+}
+
 // ---- HLLE (hydro_hlle.hpp:28-133) ----------------------------------------------------------
 // w*: (rho, v_n, v_t1, v_t2, p); gf: adjoint of the 5 flux components; gwl/gwr: output.
 __device__ void hlle_vjp(const double *wl, const double *wr, const GasConsts &gc, double ic2g,
@@ -300,30 +318,12 @@ __device__ void hlle_vjp(const double *wl, const double *wr, const GasConsts &gc
     gbp = gtmp * (-bm) * ibpm * ibpm;
     gbm = gtmp * bp * ibpm * ibpm;
   }
-  // left flux
   for (int n = 0; n < 5; ++n) gwl[n] = 0.0, gwr[n] = 0.0;
-  double gvxl = 0.0, gvxr = 0.0, gel = 0.0, ger = 0.0;
-  gwl[IDN] += gfl[0] * vxl; gvxl += gfl[0] * wl[IDN];
-  gwl[IDN] += gfl[1] * wl[IV1] * vxl; gwl[IV1] += gfl[1] * wl[IDN] * vxl;
-  gvxl += gfl[1] * wl[IDN] * wl[IV1]; gwl[IPR] += gfl[1];
-  gwl[IDN] += gfl[2] * wl[IV2] * vxl; gwl[IV2] += gfl[2] * wl[IDN] * vxl; gvxl += gfl[2] * wl[IDN] * wl[IV2];
-  gwl[IDN] += gfl[3] * wl[IV3] * vxl; gwl[IV3] += gfl[3] * wl[IDN] * vxl; gvxl += gfl[3] * wl[IDN] * wl[IV3];
-  gel += gfl[4] * vxl; gvxl += gfl[4] * el; gwl[IPR] += gfl[4] * wl[IV1]; gwl[IV1] += gfl[4] * wl[IPR];
-  // right flux
-  gwr[IDN] += gfr[0] * vxr; gvxr += gfr[0] * wr[IDN];
-  gwr[IDN] += gfr[1] * wr[IV1] * vxr; gwr[IV1] += gfr[1] * wr[IDN] * vxr;
-  gvxr += gfr[1] * wr[IDN] * wr[IV1]; gwr[IPR] += gfr[1];
-  gwr[IDN] += gfr[2] * wr[IV2] * vxr; gwr[IV2] += gfr[2] * wr[IDN] * vxr; gvxr += gfr[2] * wr[IDN] * wr[IV2];
-  gwr[IDN] += gfr[3] * wr[IV3] * vxr; gwr[IV3] += gfr[3] * wr[IDN] * vxr; gvxr += gfr[3] * wr[IDN] * wr[IV3];
-  ger += gfr[4] * vxr; gvxr += gfr[4] * er; gwr[IPR] += gfr[4] * wr[IV1]; gwr[IV1] += gfr[4] * wr[IPR];
-  // vxl = ul - bm, vxr = ur - bp
+  // fluxes of both sides (vxl = ul - bm, vxr = ur - bp)
+  const double gvxl = side_flux_vjp(wl, vxl, el, igm1, gfl, gwl);
+  const double gvxr = side_flux_vjp(wr, vxr, er, igm1, gfr, gwr);
   gwl[IV1] += gvxl; gbm -= gvxl;
   gwr[IV1] += gvxr; gbp -= gvxr;
-  // energies
-  gwl[IPR] += gel * igm1; gwl[IDN] += gel * 0.5 * kel;
-  gwl[IV1] += gel * wl[IDN] * wl[IV1]; gwl[IV2] += gel * wl[IDN] * wl[IV2]; gwl[IV3] += gel * wl[IDN] * wl[IV3];
-  gwr[IPR] += ger * igm1; gwr[IDN] += ger * 0.5 * ker;
-  gwr[IV1] += ger * wr[IDN] * wr[IV1]; gwr[IV2] += ger * wr[IDN] * wr[IV2]; gwr[IV3] += ger * wr[IDN] * wr[IV3];
   // clamps
   const double gar = bpos ? gbp : 0.0;
   const double gal = bneg ? gbm : 0.0;
@@ -397,71 +397,49 @@ __device__ void hllc_vjp(const double *wl, const double *wr, const GasConsts &gc
   const double cp0 = (ml * tr + mr * tl) * imm;
   const bool cpos = is_pos(cp0);
   const double cp = cpos ? cp0 : 0.0;
-  const double wxl = ul - bm, wxr = ur - bp;
-  double fl[5], fr[5];
-  fl[0] = rl * wxl;
-  fr[0] = rr * wxr;
-  fl[1] = rl * ul * wxl + pl;
-  fr[1] = rr * ur * wxr + pr;
-  fl[2] = rl * vl * wxl;
-  fr[2] = rr * vr * wxr;
-  fl[3] = rl * zl * wxl;
-  fr[3] = rr * zr * wxr;
-  fl[4] = el * wxl + pl * ul;
-  fr[4] = er * wxr + pr * ur;
+  // flx = c_s F_s(w_s) + (0, ustar cp, 0, 0, ustar cp sstar) with the upwind side s of the
+  // contact (left with b = bm when sstar >= 0, else right with b = bp); the other side's
+  // weight is exactly 0, so only side s is differentiated
   const bool sp = !is_neg(sstar);
-  double cl_, cr_, ustar, idn;
-  if (sp) {
-    idn = 1.0 / (sstar - bm);
-    cl_ = sstar * idn;
-    cr_ = 0.0;
-    ustar = -bm * idn;
-  } else {
-    idn = 1.0 / (bp - sstar);
-    cl_ = 0.0;
-    cr_ = -sstar * idn;
-    ustar = bp * idn;
-  }
-  // reverse: flx = cl_ fl + cr_ fr + (0, ustar cp, 0, 0, ustar cp sstar)
-  double gfl[5], gfr[5];
-  double gcl_ = 0.0, gcr_ = 0.0;
+  double ws[5];
+#pragma unroll
+  for (int n = 0; n < 5; ++n) ws[n] = sp ? wl[n] : wr[n];
+  const double b = sp ? bm : bp;
+  const double es = sp ? el : er;
+  const double wx = ws[IV1] - b;
+  double fs[5];
+  fs[0] = ws[IDN] * wx;
+  fs[1] = ws[IDN] * ws[IV1] * wx + ws[IPR];
+  fs[2] = ws[IDN] * ws[IV2] * wx;
+  fs[3] = ws[IDN] * ws[IV3] * wx;
+  fs[4] = es * wx + ws[IPR] * ws[IV1];
+  // c = sstar / (sstar - b), ustar = -b / (sstar - b)
+  const double idn = 1.0 / (sstar - b);
+  const double cs = sstar * idn;
+  const double ustar = -b * idn;
+  double gfs[5], gcs = 0.0;
 #pragma unroll
   for (int n = 0; n < 5; ++n) {
-    gfl[n] = gf[n] * cl_;
-    gfr[n] = gf[n] * cr_;
-    gcl_ += gf[n] * fl[n];
-    gcr_ += gf[n] * fr[n];
+    gfs[n] = gf[n] * cs;
+    gcs += gf[n] * fs[n];
   }
   double gustar = gf[1] * cp + gf[4] * cp * sstar;
   double gcp = gf[1] * ustar + gf[4] * ustar * sstar;
   double gsstar = gf[4] * ustar * cp;
-  double gbp = 0.0, gbm = 0.0;
-  if (sp) {
-    // cl_ = s/(s - bm), ustar = -bm/(s - bm)
-    const double i2 = idn * idn;
-    gsstar += gcl_ * (-bm) * i2 + gustar * bm * i2;
-    gbm += gcl_ * sstar * i2 + gustar * (-sstar) * i2;
-  } else {
-    // cr_ = -s/(bp - s), ustar = bp/(bp - s)
-    const double i2 = idn * idn;
-    gsstar += gcr_ * (-bp) * i2 + gustar * bp * i2;
-    gbp += gcr_ * sstar * i2 + gustar * (-sstar) * i2;
+  // d c / d sstar = -b idn^2, d c / d b = sstar idn^2; d ustar / d sstar = b idn^2,
+  // d ustar / d b = -sstar idn^2
+  const double i2 = idn * idn;
+  gsstar += (gustar - gcs) * b * i2;
+  const double gb_w = (gcs - gustar) * sstar * i2;
+  double gws[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  const double gwx = side_flux_vjp(ws, wx, es, igm1, gfs, gws);
+  gws[IV1] += gwx;
+  const double gb = gb_w - gwx;
+  for (int n = 0; n < 5; ++n) {
+    gwl[n] = sp ? gws[n] : 0.0;
+    gwr[n] = sp ? 0.0 : gws[n];
   }
-  for (int n = 0; n < 5; ++n) gwl[n] = 0.0, gwr[n] = 0.0;
-  double gwxl = 0.0, gwxr = 0.0, gel = 0.0, ger = 0.0;
-  gwl[IDN] += gfl[0] * wxl; gwxl += gfl[0] * rl;
-  gwl[IDN] += gfl[1] * ul * wxl; gwl[IV1] += gfl[1] * rl * wxl; gwxl += gfl[1] * rl * ul; gwl[IPR] += gfl[1];
-  gwl[IDN] += gfl[2] * vl * wxl; gwl[IV2] += gfl[2] * rl * wxl; gwxl += gfl[2] * rl * vl;
-  gwl[IDN] += gfl[3] * zl * wxl; gwl[IV3] += gfl[3] * rl * wxl; gwxl += gfl[3] * rl * zl;
-  gel += gfl[4] * wxl; gwxl += gfl[4] * el; gwl[IPR] += gfl[4] * ul; gwl[IV1] += gfl[4] * pl;
-  gwr[IDN] += gfr[0] * wxr; gwxr += gfr[0] * rr;
-  gwr[IDN] += gfr[1] * ur * wxr; gwr[IV1] += gfr[1] * rr * wxr; gwxr += gfr[1] * rr * ur; gwr[IPR] += gfr[1];
-  gwr[IDN] += gfr[2] * vr * wxr; gwr[IV2] += gfr[2] * rr * wxr; gwxr += gfr[2] * rr * vr;
-  gwr[IDN] += gfr[3] * zr * wxr; gwr[IV3] += gfr[3] * rr * wxr; gwxr += gfr[3] * rr * zr;
-  ger += gfr[4] * wxr; gwxr += gfr[4] * er; gwr[IPR] += gfr[4] * ur; gwr[IV1] += gfr[4] * pr;
-  // wxl = ul - bm, wxr = ur - bp
-  gwl[IV1] += gwxl; gbm -= gwxl;
-  gwr[IV1] += gwxr; gbp -= gwxr;
+  double gbm = sp ? gb : 0.0, gbp = sp ? 0.0 : gb;
   // cp = max(cp0, 0)
   const double gcp0 = cpos ? gcp : 0.0;
   // sstar = (tl - tr) imm; cp0 = (ml tr + mr tl) imm; imm = 1/(ml + mr)
@@ -486,11 +464,6 @@ __device__ void hllc_vjp(const double *wl, const double *wr, const GasConsts &gc
   // bp = sr or TINY ; bm = sl or -TINY
   if (bpos) gsr += gbp;
   if (bneg) gsl += gbm;
-  // energies
-  gwl[IPR] += gel * igm1; gwl[IDN] += gel * 0.5 * kel;
-  gwl[IV1] += gel * rl * ul; gwl[IV2] += gel * rl * vl; gwl[IV3] += gel * rl * zl;
-  gwr[IPR] += ger * igm1; gwr[IDN] += ger * 0.5 * ker;
-  gwr[IV1] += ger * rr * ur; gwr[IV2] += ger * rr * vr; gwr[IV3] += ger * rr * zr;
   // sl = ul - cl ql ; sr = ur + cr qr
   gwl[IV1] += gsl;
   double gcl = -gsl * ql, gql = -gsl * cl;
