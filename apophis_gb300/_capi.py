@@ -148,6 +148,7 @@ SIGNATURES = {
                              ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "aph_adjoint_forward_members": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _dp,
                                      ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "aph_adjoint_autotune": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "aph_adjoint_backward": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
                              ctypes.c_int),
 }

@@ -67,6 +67,10 @@ class Adjoint:
                    stream_handle())
         return out
 
+    def autotune(self, u):
+        """Tune the forward stepper's launch configuration on the state u."""
+        _capi.call("aph_adjoint_autotune", self.h, _ptr(u), stream_handle())
+
     def forward(self, u0, dts, checkpoint_every=20):
         dts = [float(x) for x in dts]
         arr = (ctypes.c_double * len(dts))(*dts)

@@ -733,7 +733,7 @@ aph_status aph_adjoint_create(const aph_stepper_desc *desc, aph_adjoint *out) {
   }
   aph_stepper_desc sd = *desc;
   sd.blocks = A->blocks.data();
-  sd.fixed_dt = 1.0;
+  sd.fixed_dt = 0.0;  // each forward step sets its dt (stepper_step_dt); the policy only tunes
   sd.tlim = 0.0;
   aph_status st = e == cudaSuccess ? aph_stepper_create(&sd, &A->st) : cuda_fail(e, "adjoint setup");
   if (st) {
@@ -827,6 +827,19 @@ aph_status aph_adjoint_forward(aph_adjoint A, const double *u0, int nsteps, cons
   for (int k = 0; k < nsteps; ++k)
     for (int m = 0; m < A->nmembers; ++m) table[(size_t)k * A->nmembers + m] = dts[k];
   return aph_adjoint_forward_members(A, u0, nsteps, table.data(), checkpoint_every, u_final, stream);
+}
+
+aph_status aph_adjoint_autotune(aph_adjoint A, const double *u, void *stream) {
+  clear_error();
+  if (!A || !u) return fail(APH_ERR_INVALID, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  // the forward stepper's launch configuration, timed on the state u (restored afterwards)
+  // (the trial steps take the CFL dt of u: the stepper's clock restarts from u)
+  cudaError_t e = cudaMemcpyAsync(A->x, u, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = stepper_restart(A->st, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint autotune");
+  return aph_stepper_autotune(A->st, 1, nullptr, nullptr);
 }
 
 aph_status aph_adjoint_backward(aph_adjoint A, const double *lam_final, double *lam_initial,

@@ -30,6 +30,8 @@ bool pack_has_topology(aph_pack p);
 cudaError_t stepper_step_dt(aph_stepper s, const double *dt_dev, double *keep, int *floor_flag,
                             cudaStream_t st);
 size_t stepper_field_doubles(aph_stepper s);
+// Clock back to zero (no end time, CFL dt policy) and the initial dt of the current state.
+cudaError_t stepper_restart(aph_stepper s, cudaStream_t st);
 
 // History sums (aph_history.cu): out_dev[0] total mass, out_dev[1] total energy; scratch
 // needs history_scratch_doubles(max_interior, nblocks) doubles (the last two hold the result).

@@ -495,8 +495,30 @@ __global__ void k_or_flags(const int *flags, int n, int *out) {
 
 }  // namespace
 
+__global__ void k_members_reset(MemberCtl *m, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    m[i].time = 0.0;
+    m[i].dt = 0.0;
+    m[i].ncycle = 0;
+    m[i].active = 1;
+    m[i].min_bits = ~0ULL;
+  }
+}
+
 namespace aph {
 size_t stepper_field_doubles(aph_stepper s) { return (size_t)5 * s->total_cells; }
+
+cudaError_t stepper_restart(aph_stepper s, cudaStream_t st) {
+  k_ctl_init<<<1, 1, 0, st>>>(s->d_ctl, DBL_MAX, 0.0);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && s->d_members) {
+    k_members_reset<<<(s->nmembers + 127) / 128, 128, 0, st>>>(s->d_members, s->nmembers);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && initial_dt(s, st) != APH_OK) e = cudaErrorUnknown;
+  return e;
+}
 
 cudaError_t stepper_step_dt(aph_stepper s, const double *dt_dev, double *keep, int *floor_flag,
                             cudaStream_t st) {

@@ -292,6 +292,7 @@ def ensemble_adjoint_leg(ckpt=20):
     torch.cuda.empty_cache()
     adj = EnsembleAdjoint(ens)
     u0 = torch.from_numpy(flat).cuda()
+    adj.autotune(u0)
     a, b, c = ev(), ev(), ev()
     a.record()
     uT = adj.forward_members(u0, dts, ckpt)
@@ -321,6 +322,7 @@ def adjoint_leg(nsteps=40):
     cfg, cons = problems.kh2d(n=512, block=64, ng=2, recon="plm", rsolver="hlle")
     u0 = torch.from_numpy(cons).cuda()
     adj = Adjoint(cfg)
+    adj.autotune(u0)
     dts = [2e-4] * nsteps
     adj.forward(u0, dts[:4], 2)
     adj.backward(torch.ones_like(u0))

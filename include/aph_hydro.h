@@ -303,6 +303,9 @@ aph_status aph_adjoint_forward(aph_adjoint adjoint, const double *u0, int nsteps
 aph_status aph_adjoint_forward_members(aph_adjoint adjoint, const double *u0, int nsteps,
                                        const double *dts, int checkpoint_every, double *u_final,
                                        void *stream);
+/* Pick the launch configuration of the adjoint's forward (its internal stepper) by timing
+ * it on the state u (as aph_stepper_autotune; blocking). */
+aph_status aph_adjoint_autotune(aph_adjoint adjoint, const double *u, void *stream);
 /* Reverse sweep of the last rollout: recompute each segment from its checkpoint, then the
  * step VJPs backwards; lam_initial = (dU^N/dU^0)^T lam_final (blocking). */
 aph_status aph_adjoint_backward(aph_adjoint adjoint, const double *lam_final, double *lam_initial,

@@ -215,3 +215,20 @@ def test_checkpoint_spacing_does_not_change_gradient(cuda):
         uT = adj.forward(cons, dts, k)
         outs.append(adj.backward(lam))
     assert torch.equal(outs[0], outs[1]) and torch.equal(outs[1], outs[2])
+
+
+def test_autotuned_forward_keeps_the_gradient(cuda):
+    """Tuning the adjoint's forward (launch shape, sweep order, staging) changes nothing the
+    taped reference can see."""
+    cfg, u = kh_setup(64, 32, "hllc", "rk2", "ppm")
+    adj = Adjoint(cfg)
+    adj.autotune(u)
+    dt = 2e-3
+    G = global_from_pack(cfg, u).requires_grad_(True)
+    ref_next = TR.step(G, dt, cfg.dx, cfg.gamma, cfg.recon, cfg.rsolver, cfg.integrator, cfg.ndim)
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    lamG = torch.randn(ref_next.shape, dtype=torch.float64, device="cuda", generator=gen)
+    (ref_vjp,) = torch.autograd.grad(ref_next, G, lamG)
+    got_vjp = global_from_pack(cfg, adj.step_vjp(u, dt, pack_from_global(cfg, lamG)))
+    assert float((got_vjp - ref_vjp).norm() / ref_vjp.norm()) < 1e-11
+    adj.close()
