@@ -1,6 +1,6 @@
 """Benchmark of the hydro flux path on one GB300.
 
-Headline workload (the BASELINE configuration that fits one GPU): 3D Kelvin-Helmholtz,
+Headline workload (the reference benchmark configuration that fits one GPU): 3D Kelvin-Helmholtz,
 256^3 periodic unit box as 64 meshblocks of 64^3 with 4 ghost cells, PPM + HLLC, RK2,
 CFL 0.3, gamma 5/3, FP64, synthetic initial data.  A "step" is one full RK2 step of the
 whole pack (2 stages + the CFL dt reduction).
