@@ -211,3 +211,17 @@ def test_ensemble_pressure_gradient_fd(cuda):
         # agreement to ~1e-6 of this cancelling sum, bounded at 1e-5
         assert abs(fd - pred) <= 1e-5 * abs(pred), (fd, pred)
     ea.close()
+
+
+def test_ensemble_tma_windows_match_plain_loads(cuda):
+    """Equal blocks across members: the TMA-staged windows give the same bits."""
+    ens, conses, flat = small_ensemble()
+    outs = []
+    for tma in (0, 1):
+        st = ensemble.EnsembleStepper(ens, flat, exact=False)
+        c = dict(st.config, tma=tma, lines=[4, 4, 0])
+        st.set_config(c)
+        st.step(4)
+        outs.append((st.state(), st.member_status()))
+        st.close()
+    assert np.array_equal(outs[0][0], outs[1][0]) and outs[0][1] == outs[1][1]
