@@ -53,7 +53,7 @@ def test_kernels_match_oracle(cuda, wl, exact):
     for d in range(cfg.ndim):
         sl = (slice(None), slice(None)) + interior_faces(cfg, d)
         ref = np.stack([ref_flux[b][d] for b in range(nb)])[sl]
-        assert_parity(md.flux[d].cpu().numpy()[sl], ref, exact, what="flux%d" % (d + 1))
+        assert_parity(md.flux[d].cpu().numpy()[sl], ref, exact, what="flux%d" % (d + 1), vector=True)
     # update from identical fluxes
     for d in range(cfg.ndim):
         md.flux[d].copy_(torch.from_numpy(np.stack([ref_flux[b][d] for b in range(nb)])))
