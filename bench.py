@@ -371,6 +371,74 @@ def cpu_baseline_amr(nsteps=2):
             "kind": "port", "sample": "%d RK2 steps of the RT pack after 1 warm-up" % nsteps}
 
 
+def table_leg(args):
+    """Zone-updates/s of every configuration on every path, for the results table: the CPU
+    oracle (host cores), the plain path per meshblock and per pack, and the batched stepper
+    (rank 0; bounded samples)."""
+    import torch
+    from apophis_gb300 import ensemble, hydro, problems
+    from apophis_gb300.stepper import Stepper
+    from oracle import oracle as O
+
+    def gpu_time(fn, n):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn(n)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / n
+
+    def uniform_rows(name, cfg, cons, nsteps, fixed_dt=0.0):
+        zones = cfg.zones()
+        out = {"workload": name, "zones": zones}
+        m = O.Mesh(cfg)
+        m.set_cons(cons)
+        m.run(nsteps=1, fixed_dt=fixed_dt)
+        t = time.perf_counter()
+        m.run(nsteps=nsteps, fixed_dt=fixed_dt)
+        out["cpu_oracle"] = zones * nsteps / (time.perf_counter() - t)
+        out["cpu_cores"] = O.num_threads()
+        for label, per_block, n in (("gpu_plain_per_meshblock", True, max(1, nsteps // 2)),
+                                    ("gpu_plain_per_pack", False, nsteps)):
+            d = hydro.Driver(cfg, cons, exact=False, per_block=per_block)
+            d.run(nsteps=1, fixed_dt=fixed_dt)
+            out[label] = zones / gpu_time(lambda k: d.run(nsteps=k, fixed_dt=fixed_dt), n)
+            d.md.close()
+        st = Stepper(cfg, cons, exact=False, fixed_dt=fixed_dt)
+        st.autotune(trial_steps=1)
+        st.step(3)
+        st.status()
+        out["gpu_batched_graph"] = zones / gpu_time(lambda k: (st.step(k), st.status()), 4 * nsteps)
+        st.close()
+        torch.cuda.empty_cache()
+        return out
+
+    rows = []
+    cfg, cons = problems.sod(nx=256, recon="plm", rsolver="hlle", integrator="rk2", cfl=0.4)
+    rows.append(uniform_rows("sod 1D 256 cells, PLM+HLLE, RK2", cfg, cons, 50))
+    cfg, cons = problems.kh2d(n=512, block=64, ng=2, recon="plm", rsolver="hlle")
+    rows.append(uniform_rows("kh2d 512^2 (64 x 64^2), PLM+HLLE, RK2", cfg, cons, 10, fixed_dt=2e-4))
+    # the blast ensemble: every member on the CPU oracle and the per-pack plain path
+    ens, flat = ensemble.blast_ensemble()
+    zones = ens.zones()
+    t_cpu = 0.0
+    t_pack = 0.0
+    for m_i, mcfg in enumerate(ens.members):
+        mcons = ens.unpack(flat, m_i)
+        m = O.Mesh(mcfg)
+        m.set_cons(mcons)
+        t = time.perf_counter()
+        m.run(nsteps=1)
+        t_cpu += time.perf_counter() - t
+        d = hydro.Driver(mcfg, mcons, exact=False)
+        d.run(nsteps=1)
+        t_pack += gpu_time(lambda k: d.run(nsteps=k), 2)
+        d.md.close()
+    rows.append({"workload": "blast ensemble, 64 members, PPM+HLLC, RK2 (one step of every member)",
+                 "zones": zones, "cpu_oracle": zones / t_cpu, "cpu_cores": O.num_threads(),
+                 "gpu_plain_per_pack": zones / t_pack})
+    return rows
+
+
 def run_reference(args, cfg, cons):
     dist, rank, ws = dist_init()
     if rank != 0:
@@ -400,7 +468,7 @@ def main():
     ap.add_argument("--no-amr", action="store_true", help="skip the refined-pack leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint ratio leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the blast-ensemble leg")
-    ap.add_argument("--only", choices=["amr", "ensemble", "adjoint"],
+    ap.add_argument("--only", choices=["amr", "ensemble", "adjoint", "table"],
                     help="run one extra leg alone and print its object (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -410,7 +478,7 @@ def main():
         from apophis_gb300 import _build
         _build.build()
         out = {"amr": lambda: amr_leg(args, args.warmup), "ensemble": lambda: ensemble_leg(args),
-               "adjoint": adjoint_leg}[args.only]()
+               "adjoint": adjoint_leg, "table": lambda: table_leg(args)}[args.only]()
         print(json.dumps({"only": args.only, args.only: out}), flush=True)
         return
 
