@@ -327,12 +327,16 @@ aph_status configure(aph_stepper s) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  s->grid = per_sm * sms;
   // entire-domain cell chunks
   std::vector<int2> cells;
   for (int b = 0; b < nb; ++b)
     for (long long c = 0; c < s->hblocks[b].ncell; c += threads) cells.push_back(make_int2(b, (int)c));
   s->ncell_items = (int)cells.size();
+  // no more CTAs than the largest phase has work items: a small pack (one Sod block) then
+  // waits at its grid barriers for a few CTAs instead of a full GPU's worth
+  int most = std::max(s->ncell_items, s->nfix_items);
+  for (int d = 0; d < p.ndim; ++d) most = std::max(most, s->nline_items[d]);
+  s->grid = std::max(1, std::min(per_sm * sms, most));
   return upload_items(s, &s->d_cell_items, cells);
 }
 
