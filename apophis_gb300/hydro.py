@@ -56,14 +56,14 @@ class MeshData:
         _capi.load()
         self.cfg = cfg
         self.exact = exact
-        shape = cfg.pack_shape(5)
+        shape = cfg.pack_shape(cfg.nvar)
         kw = dict(dtype=torch.float64, device=device)
         self.cons = torch.zeros(shape, **kw)
         self.prim = torch.zeros(shape, **kw)
         self.u1 = torch.zeros(shape, **kw)
         self.gamma = torch.zeros(shape[:1] + (2,) + shape[2:], **kw)
         self.flux = [torch.zeros(shape, **kw) if d < cfg.ndim else None for d in range(3)]
-        self.params = make_params(cfg, exact)
+        self.params = make_params(cfg, exact, cfg.nvar)
         self.pack = self._make_pack(range(cfg.nblocks))
         nb = (ctypes.c_int * 3)(*cfg.blocks_per_dim)
         bc = (ctypes.c_int * 6)(*[_capi.BC[cfg.bc[d][s]] for d in range(3) for s in range(2)])

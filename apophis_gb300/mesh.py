@@ -42,6 +42,7 @@ class MeshConfig:
     pfloor: float = DEFAULT_FLOOR
     gravity: Optional[Tuple[float, float, float]] = None
     name: str = field(default="mesh")
+    nscalars: int = 0   # passive scalars (hydro/composition), conserved as rho * s
 
     def __post_init__(self):
         self.mesh_nx = tuple(int(x) for x in self.mesh_nx)
@@ -57,6 +58,10 @@ class MeshConfig:
     @property
     def gm1(self):
         return self.gamma - 1.0
+
+    @property
+    def nvar(self):
+        return NHYDRO + self.nscalars
 
     @property
     def blocks_per_dim(self):

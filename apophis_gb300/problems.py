@@ -228,3 +228,25 @@ class LinearWave:
             l1 += diff.reshape(5, -1).sum(axis=1) * vol
         l1 /= 3.0 * 1.5 * 1.5
         return float(np.sqrt(np.sum(l1 * l1))), l1
+
+
+def kh2d_tracers(n=64, block=32, ng=2, recon="plm", rsolver="hllc", integrator="rk2", cfl=0.3,
+                 gamma=5.0 / 3.0, nscalars=2):
+    """kh2d_smooth with passive scalars (dyes) advected by the flow: scalar k is
+    rho * s_k with s_0 marking the central band and s_1 a smooth pattern in x and y."""
+    base, cons5 = kh2d_smooth(n=n, block=block, ng=ng, recon=recon, rsolver=rsolver,
+                              integrator=integrator, cfl=cfl, gamma=gamma)
+    cfg = MeshConfig(ndim=2, mesh_nx=base.mesh_nx, block_nx=base.block_nx, ng=ng, recon=recon,
+                     rsolver=rsolver, integrator=integrator, cfl=cfl, gamma=gamma,
+                     name="kh2d_tracers", nscalars=nscalars)
+    cons = np.zeros(cfg.pack_shape(cfg.nvar))
+    cons[:, :5] = cons5
+    sk, sj, si = cfg.interior
+    for b in range(cfg.nblocks):
+        x, y, _ = cfg.cell_centers(b)
+        rho = cons5[b, 0][sk, sj, si]
+        dyes = [0.5 * (np.tanh((y - 0.25) / 0.05) - np.tanh((y - 0.75) / 0.05)),
+                0.5 + 0.25 * np.sin(2 * math.pi * x) * np.cos(2 * math.pi * y)]
+        for k in range(nscalars):
+            cons[b, 5 + k][sk, sj, si] = rho * dyes[k % 2]
+    return cfg, cons

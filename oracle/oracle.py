@@ -122,7 +122,7 @@ class Mesh:
         self.cfg = cfg
         nbx = cfg.blocks_per_dim
         bc = cfg.bc
-        ints = [5, cfg.ndim, cfg.block_nx[0], cfg.block_nx[1], cfg.block_nx[2],
+        ints = [cfg.nvar, cfg.ndim, cfg.block_nx[0], cfg.block_nx[1], cfg.block_nx[2],
                 nbx[0], nbx[1], nbx[2], cfg.ng, RECON[cfg.recon], RSOLVER[cfg.rsolver],
                 INTEGRATOR[cfg.integrator],
                 BC[bc[0][0]], BC[bc[0][1]], BC[bc[1][0]], BC[bc[1][1]], BC[bc[2][0]],
@@ -132,7 +132,7 @@ class Mesh:
         self._ints = (ctypes.c_int * len(ints))(*ints)
         self._reals = (ctypes.c_double * len(reals))(*reals)
         self.h = lib().orc_mesh_create(self._ints, self._reals)
-        self.shape = cfg.pack_shape(5)
+        self.shape = cfg.pack_shape(cfg.nvar)
 
     def __del__(self):
         if getattr(self, "h", None):
