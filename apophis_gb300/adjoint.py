@@ -32,7 +32,7 @@ class Adjoint:
             blocks[b].cons = 1  # unused by the adjoint, must be non-null
         self._blocks = blocks
         desc = _capi.aph_stepper_desc()
-        desc.params = make_params(cfg, exact=False)
+        desc.params = make_params(cfg, exact=False, nvar=cfg.nvar)
         desc.integrator = _capi.INTEGRATOR[cfg.integrator]
         desc.nblocks = cfg.nblocks
         desc.blocks = ctypes.cast(blocks, ctypes.POINTER(_capi.aph_block))

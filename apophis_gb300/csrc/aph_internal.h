@@ -143,8 +143,8 @@ APH_DECLARE_LAUNCHERS(aph_exact)
 
 #define APH_DECLARE_STAGE(NS)                                                                  \
   namespace NS {                                                                               \
-  size_t stage_smem_bytes(int recon, int n, int T);                                            \
-  size_t stage_smem_bytes_tma(int recon, int n, int T, int L);                                 \
+  size_t stage_smem_bytes(int recon, int n, int T, int nvar);                                  \
+  size_t stage_smem_bytes_tma(int recon, int n, int T, int L, int nvar);                       \
   const void *stage_kernel(int recon, int rsolver);                                            \
   cudaError_t launch_stage(const aph::StageArgs &a, int recon, int rsolver, int grid,          \
                            int threads, size_t smem, bool cooperative, int reg_cap,            \

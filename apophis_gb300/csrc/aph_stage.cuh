@@ -200,6 +200,7 @@ __device__ void ghost_cell(const StageArgs &a, const StepBlock &B, long long c) 
     if ((n == IM1 && flip[0]) || (n == IM2 && flip[1]) || (n == IM3 && flip[2])) v = -v;
     B.u0[n * B.ncell + c] = v;
   }
+  for (int n = NHYDRO; n < p.nvar; ++n) B.u0[n * B.ncell + c] = S.u0[n * S.ncell + sc];
 }
 
 __device__ __forceinline__ bool is_interior(const PackDev &p, const StepBlock &B, long long c,
@@ -309,10 +310,12 @@ __host__ __device__ constexpr size_t pass_smem_doubles(int recon, int n, int T, 
              : (size_t)V * T * ((n + 2 * (recon == RECON_PLM ? 2 : 1)) + 2 * (n + 2));
 }
 
-// Doubles between the window region and the TMA staging area: the window is padded to a
-// multiple of 16 doubles so that the staging area starts 128-byte aligned.
-__host__ __device__ constexpr size_t tma_stage_offset(int recon, int n, int T) {
-  return ((size_t)7 * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1)) + 15) / 16 * 16;
+// Doubles between the window region and the TMA staging area: the window (nvar + 2
+// variables) is padded to a multiple of 16 doubles so that the staging area starts 128-byte
+// aligned.
+__host__ __device__ constexpr size_t tma_stage_offset(int recon, int n, int T, int nvar) {
+  return ((size_t)(nvar + 2) * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1)) + 15) /
+         16 * 16;
 }
 
 // One pass item: lines l0..l0+nl-1 of block B along DIR.  b: the block's index in the pack;
@@ -323,7 +326,8 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
                           unsigned long long &dtmin, unsigned mbar, unsigned &tma_phase) {
   constexpr int G = Halo<RECON>::G;
   const int n = B.nx[DIR - 1];
-  const int V = constg ? 5 : 7;
+  const int nv = a.p.nvar;  // 5 hydro variables, then the passive scalars
+  const int V = constg ? nv : nv + 2;  // with gamma_c, gamma_e where the gas is not ideal
   const GasConsts gc = gas_of(a, B);
   const int NW = n + 2 * G;
   const long long nc = B.ncell;
@@ -343,7 +347,7 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
     // one tensor copy of the T lines' whole extent into the staging area, then the window
     // cells -G..n+G-1 into W (the staging layout is [v][t][i] along x, [v][w][t] along y, z)
     // 128-byte aligned staging area after the window region (the size reserves the slack)
-    double *stg = (double *)(((unsigned long long)(sm + tma_stage_offset(RECON, n, T)) + 127ULL) & ~127ULL);
+    double *stg = (double *)(((unsigned long long)(sm + tma_stage_offset(RECON, n, T, nv)) + 127ULL) & ~127ULL);
     const int L = a.ext[DIR - 1];
     const int ng = a.p.ng;
     // order every thread's earlier generic accesses of this shared memory before the copy
@@ -354,7 +358,7 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
     const int per_plane = DIR == 1 ? B.nx[1] : B.nx[0];
     const int lp = l0 % per_plane, plane = l0 / per_plane;
     const int T1 = min(nl, per_plane - lp);
-    const size_t box = (size_t)NHYDRO * T * L;
+    const size_t box = (size_t)nv * T * L;
     if (tid == 0) {
       const unsigned bytes = (unsigned)((nl > T1 ? 2 : 1) * box * sizeof(double));
       mbar_expect_tx(mbar, bytes);
@@ -370,7 +374,7 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
     }
     mbar_wait_bounded(mbar, tma_phase, a.ctl, a.timeout_ns);
     tma_phase ^= 1u;
-    for (int it = tid; it < NHYDRO * nl * NW; it += nth) {
+    for (int it = tid; it < nv * nl * NW; it += nth) {
       const int v = it / (nl * NW);
       const int r = it - v * nl * NW;
       const int t = r / NW, w = r - t * NW;
@@ -389,7 +393,7 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
       if (DIR == 1) { t = r / NW; w = r - t * NW; } else { w = r / nl; t = r - w * nl; }
       long long base, stride, ib, is;
       line_of<DIR>(B, a.p.ndim, a.p.ng, l0 + t, base, stride, ib, is);
-      const double *src = v < NHYDRO ? B.prim + v * nc : B.gamma + (v - NHYDRO) * nc;
+      const double *src = v < nv ? B.prim + v * nc : B.gamma + (v - nv) * nc;
       W[((size_t)v * T + t) * NW + w] = src[base + (long long)(w - G) * stride];
     }
   }
@@ -462,14 +466,14 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
       wr[IDN] = SR[IDN * vs + oR]; wr[IV1] = SR[ivx * vs + oR]; wr[IV2] = SR[ivy * vs + oR];
       wr[IV3] = SR[ivz * vs + oR]; wr[IPR] = SR[IPR * vs + oR];
 #if APH_EXACT
-      riemann<RS, false>(wl, wr, SL[5 * vs + oL], SL[6 * vs + oL], SR[5 * vs + oR],
-                         SR[6 * vs + oR], gc, flx);
+      riemann<RS, false>(wl, wr, SL[nv * vs + oL], SL[(nv + 1) * vs + oL], SR[nv * vs + oR],
+                         SR[(nv + 1) * vs + oR], gc, flx);
 #else
       if (constg) {
         riemann<RS, true>(wl, wr, 0.0, 0.0, 0.0, 0.0, gc, flx);
       } else {
-        riemann<RS, false>(wl, wr, SL[5 * vs + oL], SL[6 * vs + oL], SR[5 * vs + oR],
-                           SR[6 * vs + oR], gc, flx);
+        riemann<RS, false>(wl, wr, SL[nv * vs + oL], SL[(nv + 1) * vs + oL], SR[nv * vs + oR],
+                           SR[(nv + 1) * vs + oR], gc, flx);
       }
 #endif
       // store in cons order
@@ -480,6 +484,9 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
       F[ivy * fs + of] = flx[IV2];
       F[ivz * fs + of] = flx[IV3];
       F[IEN * fs + of] = flx[IEN];
+      // passive scalars: upwind by the mass flux (hydro.cpp:607-615)
+      for (int v = NHYDRO; v < nv; ++v)
+        F[v * fs + of] = flx[IDN] * (!is_neg(flx[IDN]) ? SL[v * vs + oL] : SR[v * vs + oR]);
     }
   }
   __syncthreads();
@@ -498,7 +505,7 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
     const size_t fs = (size_t)T * w1;
     const double area = DIR == 1 ? B.dx[1] * B.dx[2] : DIR == 2 ? B.dx[0] * B.dx[2] : B.dx[0] * B.dx[1];
     if (!last_pass || a.cf) {
-      for (int it = tid; it < NHYDRO * nl * n; it += nth) {
+      for (int it = tid; it < nv * nl * n; it += nth) {
         const int v = it / (nl * n);
         const int r = it - v * nl * n;
         const int t = r / n, c = r - t * n;
@@ -535,6 +542,20 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
 #endif
           u[v] = a.gam0 * B.u0[v * nc + cell] + a.gam1 * B.u1[v * nc + cell] + beta_dt * div;
         }
+        bool bad = false;
+        for (int v = NHYDRO; v < nv; ++v) {  // passive scalars
+          const size_t of = v * fs + (size_t)t * w1 + c;
+          double du = (area * F[of + 1] - area * F[of]);
+          if (!first_pass) du = B.du[v * B.nint + icell] + du;
+#if APH_EXACT
+          const double div = -du / vol;
+#else
+          const double div = -du * ivol;
+#endif
+          const double q = a.gam0 * B.u0[v * nc + cell] + a.gam1 * B.u1[v * nc + cell] + beta_dt * div;
+          B.u0[v * nc + cell] = q;
+          bad |= ((__double_as_longlong(q) >> 52) & 0x7ff) == 0x7ff;
+        }
         if (a.gravity) {  // ApplyGravity with the stage input's prim (gravity.cpp:386-407)
           const double rho = B.prim[IDN * nc + cell];
           u[IM1] += a.grav[0] * rho * beta_dt;
@@ -549,7 +570,6 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
           }
           u[IEN] += de * rho * beta_dt;
         }
-        bool bad = false;
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v) {
           B.u0[v * nc + cell] = u[v];
@@ -719,6 +739,14 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
     for (int n = 0; n < NHYDRO; ++n) B.prim[n * nc + c] = wv[n];
     B.gamma[c] = g_c;
     B.gamma[nc + c] = g_e;
+    if (p.nvar > NHYDRO) {  // passive scalars: concentration = cons / floored density
+      const double di = 1.0 / u[IDN];
+      for (int n = NHYDRO; n < p.nvar; ++n) {
+        const double q = B.u0[n * nc + c];
+        B.prim[n * nc + c] = q * di;
+        if (a.copy_u1 && inner) B.u1[n * nc + c] = q;
+      }
+    }
     if (fl) atomicOr(&a.block_flags[w.x], 1);
     if (a.copy_u1 && inner) {
 #pragma unroll
@@ -785,17 +813,17 @@ cudaError_t launch_barrier_probe(StepCtl *ctl, unsigned long long timeout_ns, cu
   return cudaGetLastError();
 }
 
-size_t stage_smem_bytes(int recon, int n, int T) {
-  return pass_smem_doubles(recon, n, T, 7) * sizeof(double);
+size_t stage_smem_bytes(int recon, int n, int T, int nvar) {
+  return pass_smem_doubles(recon, n, T, nvar + 2) * sizeof(double);
 }
 
 // With TMA staging: the window region padded to 128 bytes, then the larger of the remaining
-// pass regions and the staging area (5 variables x T lines x the line's entire extent L).
-size_t stage_smem_bytes_tma(int recon, int n, int T, int L) {
-  const size_t rest = pass_smem_doubles(recon, n, T, 7) -
-                      (size_t)7 * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1));
-  const size_t stage = (size_t)2 * NHYDRO * T * L;  // two boxes for items that cross a plane
-  return (tma_stage_offset(recon, n, T) + 16 + (rest > stage ? rest : stage)) * sizeof(double);
+// pass regions and the staging area (nvar variables x T lines x the line's entire extent L).
+size_t stage_smem_bytes_tma(int recon, int n, int T, int L, int nvar) {
+  const size_t rest = pass_smem_doubles(recon, n, T, nvar + 2) -
+                      (size_t)(nvar + 2) * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1));
+  const size_t stage = (size_t)2 * nvar * T * L;  // two boxes for items that cross a plane
+  return (tma_stage_offset(recon, n, T, nvar) + 16 + (rest > stage ? rest : stage)) * sizeof(double);
 }
 
 template <int RECON, int MINB>

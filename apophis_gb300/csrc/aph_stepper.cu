@@ -236,15 +236,15 @@ aph_status encode_tmaps(aph_stepper s) {
   }
   const StepBlock &B0 = s->hblocks[0];
   const PackDev &p = s->dev;
-  const cuuint64_t dims[5] = {(cuuint64_t)B0.ni, (cuuint64_t)B0.nj, (cuuint64_t)B0.nk, 5,
-                              (cuuint64_t)p.nblocks};
+  const cuuint64_t dims[5] = {(cuuint64_t)B0.ni, (cuuint64_t)B0.nj, (cuuint64_t)B0.nk,
+                              (cuuint64_t)p.nvar, (cuuint64_t)p.nblocks};
   const cuuint64_t strides[4] = {(cuuint64_t)B0.ni * 8, (cuuint64_t)B0.ni * B0.nj * 8,
-                                 (cuuint64_t)B0.ncell * 8, (cuuint64_t)B0.ncell * 5 * 8};
+                                 (cuuint64_t)B0.ncell * 8, (cuuint64_t)B0.ncell * p.nvar * 8};
   const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
   CUtensorMap maps[3];
   std::memset(maps, 0, sizeof(maps));
   for (int d = 0; d < 3; ++d) {
-    cuuint32_t box[5] = {1, 1, 1, 5, 1};
+    cuuint32_t box[5] = {1, 1, 1, (cuuint32_t)p.nvar, 1};
     const int T = std::max(1, s->T[d]);
     if (d == 0) { box[0] = B0.ni; box[1] = T; }
     else if (d == 1) { box[0] = T; box[1] = B0.nj; }
@@ -280,10 +280,11 @@ aph_status configure(aph_stepper s) {
     T = std::min(T, ntr_max);
     s->T[d] = T;
     const int ext = d == 0 ? s->hblocks[0].ni : d == 1 ? s->hblocks[0].nj : s->hblocks[0].nk;
-    const size_t need = s->cfg.tma ? (s->params.exact ? aph_exact::stage_smem_bytes_tma(recon, n, T, ext)
-                                                      : aph_fast::stage_smem_bytes_tma(recon, n, T, ext))
-                                   : (s->params.exact ? aph_exact::stage_smem_bytes(recon, n, T)
-                                                      : aph_fast::stage_smem_bytes(recon, n, T));
+    const int nv = p.nvar;
+    const size_t need = s->cfg.tma ? (s->params.exact ? aph_exact::stage_smem_bytes_tma(recon, n, T, ext, nv)
+                                                      : aph_fast::stage_smem_bytes_tma(recon, n, T, ext, nv))
+                                   : (s->params.exact ? aph_exact::stage_smem_bytes(recon, n, T, nv)
+                                                      : aph_fast::stage_smem_bytes(recon, n, T, nv));
     smem = std::max(smem, need);
     std::vector<int2> items;
     // schedule order: largest blocks first (longest-processing-time) so that the tail of a
@@ -511,7 +512,7 @@ __global__ void k_members_reset(MemberCtl *m, int n) {
 }
 
 namespace aph {
-size_t stepper_field_doubles(aph_stepper s) { return (size_t)5 * s->total_cells; }
+size_t stepper_field_doubles(aph_stepper s) { return (size_t)s->dev.nvar * s->total_cells; }
 
 cudaError_t stepper_restart(aph_stepper s, cudaStream_t st) {
   k_ctl_init<<<1, 1, 0, st>>>(s->d_ctl, DBL_MAX, 0.0);
@@ -553,15 +554,16 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   if (!desc || !out) return fail(APH_ERR_INVALID, "NULL argument");
   *out = nullptr;
   if (aph_status st = validate_params(&desc->params)) return st;
-  if (desc->params.nvar != 5)
-    return fail(APH_ERR_UNSUPPORTED, "the batched stepper carries no passive scalars (nvar 5)");
   if (stages_of(desc->integrator).empty())
     return fail(APH_ERR_INVALID, "integrator %d not recognized", desc->integrator);
   if (desc->nblocks <= 0 || !desc->blocks) return fail(APH_ERR_INVALID, "no blocks");
   const int ndim = desc->params.ndim;
   const bool amr = desc->amr != nullptr;
+  const int nvar = desc->params.nvar;
   if (amr) {
     if (ndim != 2) return fail(APH_ERR_UNSUPPORTED, "refined meshes are 2D");
+    if (nvar != 5)
+      return fail(APH_ERR_UNSUPPORTED, "packs with face tables carry no passive scalars (nvar 5)");
     std::vector<AmrFaces> faces(desc->nblocks);
     std::vector<int> nxs(2 * desc->nblocks);
     for (int b = 0; b < desc->nblocks; ++b) {
@@ -627,7 +629,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   p.nblocks = desc->nblocks;
   p.ndim = ndim;
   p.ng = desc->params.nghost;
-  p.nvar = 5;
+  p.nvar = nvar;
   p.gm1 = desc->params.gm1;
   p.dfloor = desc->params.dfloor;
   p.pfloor = desc->params.pfloor;
@@ -711,10 +713,10 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   s->cfg.tma = 0;
   cudaError_t e = cudaSuccess;
   auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-  ck(cudaMalloc(&s->d_u1, sizeof(double) * 5 * cells));
-  ck(cudaMalloc(&s->d_prim, sizeof(double) * 5 * cells));
+  ck(cudaMalloc(&s->d_u1, sizeof(double) * nvar * cells));
+  ck(cudaMalloc(&s->d_prim, sizeof(double) * nvar * cells));
   ck(cudaMalloc(&s->d_gamma, sizeof(double) * 2 * cells));
-  ck(cudaMalloc(&s->d_du, sizeof(double) * 5 * inter));
+  ck(cudaMalloc(&s->d_du, sizeof(double) * nvar * inter));
   ck(cudaMalloc(&s->d_flags, sizeof(int) * p.nblocks));
   ck(cudaMalloc(&s->d_ctl, sizeof(StepCtl)));
   ck(cudaMalloc(&s->d_blocks, sizeof(StepBlock) * p.nblocks));
@@ -749,10 +751,10 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   long long oc = 0, oi = 0;
   for (int b = 0; b < p.nblocks; ++b) {
     StepBlock &B = s->hblocks[b];
-    B.u1 = s->d_u1 + 5 * oc;
-    B.prim = s->d_prim + 5 * oc;
+    B.u1 = s->d_u1 + (size_t)nvar * oc;
+    B.prim = s->d_prim + (size_t)nvar * oc;
     B.gamma = s->d_gamma + 2 * oc;
-    B.du = s->d_du + 5 * oi;
+    B.du = s->d_du + (size_t)nvar * oi;
     if (amr) B.bflux = s->d_bflux + (size_t)4 * s->bflux_stride * b;
     oc += B.ncell;
     oi += B.nint;
@@ -980,9 +982,10 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_fail(e, "autotune");
   // back up u0 of every block and the control block
-  const size_t nb5 = sizeof(double) * 5;
+  const int nv = s->dev.nvar;
+  const size_t nbv = sizeof(double) * nv;
   if (!s->d_backup) {
-    e = cudaMalloc(&s->d_backup, nb5 * s->total_cells);
+    e = cudaMalloc(&s->d_backup, nbv * s->total_cells);
     if (e != cudaSuccess) return cuda_fail(e, "autotune backup");
   }
   StepCtl ctl_saved;
@@ -993,14 +996,14 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
                    cudaMemcpyDeviceToHost);
   long long off = 0;
   for (const StepBlock &B : s->hblocks) {
-    if (e == cudaSuccess) e = cudaMemcpy(s->d_backup + 5 * off, B.u0, nb5 * B.ncell, cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_backup + nv * off, B.u0, nbv * B.ncell, cudaMemcpyDeviceToDevice);
     off += B.ncell;
   }
   if (e != cudaSuccess) return cuda_fail(e, "autotune backup");
   auto restore = [&]() {
     long long o = 0;
     for (const StepBlock &B : s->hblocks) {
-      cudaMemcpy(B.u0, s->d_backup + 5 * o, nb5 * B.ncell, cudaMemcpyDeviceToDevice);
+      cudaMemcpy(B.u0, s->d_backup + nv * o, nbv * B.ncell, cudaMemcpyDeviceToDevice);
       o += B.ncell;
     }
     cudaMemcpy(s->d_ctl, &ctl_saved, sizeof(StepCtl), cudaMemcpyHostToDevice);

@@ -19,15 +19,21 @@ PRIM_NAMES = ["density", "velocity_x", "velocity_y", "velocity_z", "pressure"]
 
 
 def write_dump(base, cfg: MeshConfig, cons, time=0.0, ncycle=0, prim=None):
-    """cons (and optionally prim): (nblocks, 5, nk, nj, ni) with ghosts, numpy or torch."""
+    """cons (and optionally prim): (nblocks, nvar, nk, nj, ni) with ghosts, numpy or torch;
+    components past the fifth are passive scalars."""
     def interior(a):
         a = a.detach().cpu().numpy() if hasattr(a, "detach") else np.asarray(a)
         sk, sj, si = cfg.interior
         return np.ascontiguousarray(a[:, :, sk, sj, si], dtype="<f8")
 
-    sets = [("cons", interior(cons), CONS_NAMES)]
+    def names(base, a):
+        return base + ["scalar_%d" % k for k in range(a.shape[1] - len(base))]
+
+    c = interior(cons)
+    sets = [("cons", c, names(CONS_NAMES, c))]
     if prim is not None:
-        sets.append(("prim", interior(prim), PRIM_NAMES))
+        w = interior(prim)
+        sets.append(("prim", w, names(PRIM_NAMES, w)))
     meta = {
         "format": "apophis_gb300 dump 1",
         "Time": float(time), "NCycle": int(ncycle),

@@ -7,6 +7,7 @@ the reference's problem generators: src/pgen/sod.cpp:11-46, kh.cpp:71-119,
 rt.cpp:18-104, blast.cpp:16-71, linear_wave.cpp:42-147 and 304-419.
 Random perturbations come from numpy's PCG64 generator with a fixed seed.
 """
+import dataclasses
 import math
 
 import numpy as np
@@ -230,23 +231,30 @@ class LinearWave:
         return float(np.sqrt(np.sum(l1 * l1))), l1
 
 
+def with_tracers(cfg, cons5, nscalars=2):
+    """(cfg, cons) of any problem with passive scalars (dyes) added: scalar k is rho * s_k,
+    s_0 a band in y (in x for 1D) and s_1 a smooth pattern in x, y, z, s_2 = s_0 ..."""
+    tcfg = dataclasses.replace(cfg, nscalars=nscalars)
+    cons = np.zeros(tcfg.pack_shape(tcfg.nvar))
+    cons[:, :5] = cons5[:, :5]
+    sk, sj, si = tcfg.interior
+    for b in range(tcfg.nblocks):
+        x, y, z = tcfg.cell_centers(b)
+        rho = cons5[b, 0][sk, sj, si]
+        q = y if tcfg.ndim >= 2 else x
+        dyes = [0.5 * (np.tanh((q - 0.25) / 0.05) - np.tanh((q - 0.75) / 0.05)),
+                0.5 + 0.25 * np.sin(2 * math.pi * x) * np.cos(2 * math.pi * y) * np.cos(2 * math.pi * z)]
+        for k in range(nscalars):
+            cons[b, 5 + k][sk, sj, si] = rho * dyes[k % 2]
+    return tcfg, cons
+
+
 def kh2d_tracers(n=64, block=32, ng=2, recon="plm", rsolver="hllc", integrator="rk2", cfl=0.3,
                  gamma=5.0 / 3.0, nscalars=2):
     """kh2d_smooth with passive scalars (dyes) advected by the flow: scalar k is
     rho * s_k with s_0 marking the central band and s_1 a smooth pattern in x and y."""
-    base, cons5 = kh2d_smooth(n=n, block=block, ng=ng, recon=recon, rsolver=rsolver,
-                              integrator=integrator, cfl=cfl, gamma=gamma)
-    cfg = MeshConfig(ndim=2, mesh_nx=base.mesh_nx, block_nx=base.block_nx, ng=ng, recon=recon,
-                     rsolver=rsolver, integrator=integrator, cfl=cfl, gamma=gamma,
-                     name="kh2d_tracers", nscalars=nscalars)
-    cons = np.zeros(cfg.pack_shape(cfg.nvar))
-    cons[:, :5] = cons5
-    sk, sj, si = cfg.interior
-    for b in range(cfg.nblocks):
-        x, y, _ = cfg.cell_centers(b)
-        rho = cons5[b, 0][sk, sj, si]
-        dyes = [0.5 * (np.tanh((y - 0.25) / 0.05) - np.tanh((y - 0.75) / 0.05)),
-                0.5 + 0.25 * np.sin(2 * math.pi * x) * np.cos(2 * math.pi * y)]
-        for k in range(nscalars):
-            cons[b, 5 + k][sk, sj, si] = rho * dyes[k % 2]
+    cfg, cons5 = kh2d_smooth(n=n, block=block, ng=ng, recon=recon, rsolver=rsolver,
+                             integrator=integrator, cfl=cfl, gamma=gamma)
+    cfg, cons = with_tracers(cfg, cons5, nscalars)
+    cfg.name = "kh2d_tracers"
     return cfg, cons

@@ -3,7 +3,7 @@ include/aph_hydro.h).
 
 Each RK stage is one persistent launch over every meshblock; dt and time stay on the
 device; a step is captured once as a CUDA graph and replayed.  ``Stepper`` owns the
-state tensor ``cons`` (nblocks, 5, nk, nj, ni); the C library owns the rest.
+state tensor ``cons`` (nblocks, nvar, nk, nj, ni); the C library owns the rest.
 Launch configurations found by ``autotune`` are cached in a JSON file keyed by the
 workload and the GPU.
 """
@@ -29,7 +29,7 @@ class Stepper:
         self.cfg = cfg
         self.exact = exact
         if cons is None:
-            cons = torch.zeros(cfg.pack_shape(5), dtype=torch.float64, device="cuda")
+            cons = torch.zeros(cfg.pack_shape(cfg.nvar), dtype=torch.float64, device="cuda")
             cons.copy_(torch.as_tensor(np.ascontiguousarray(cons0)))
         self.cons = cons
         blocks = (_capi.aph_block * cfg.nblocks)()
@@ -40,7 +40,7 @@ class Stepper:
                 blocks[b].dx[d] = cfg.dx[d]
         self._blocks = blocks
         desc = _capi.aph_stepper_desc()
-        desc.params = make_params(cfg, exact)
+        desc.params = make_params(cfg, exact, cfg.nvar)
         desc.integrator = _capi.INTEGRATOR[cfg.integrator]
         desc.nblocks = cfg.nblocks
         desc.blocks = ctypes.cast(blocks, ctypes.POINTER(_capi.aph_block))
@@ -91,7 +91,7 @@ class Stepper:
         and its clock."""
         from . import output
         d = output.Dump(base)
-        cons = np.zeros(cfg.pack_shape(5))
+        cons = np.zeros(cfg.pack_shape(cfg.nvar))
         sk, sj, si = cfg.interior
         cons[:, :, sk, sj, si] = d.Get("cons", flatten=False)
         st = cls(cfg, cons, exact=bool(d.meta.get("Exact", 0)) if exact is None else exact, tlim=tlim)
@@ -137,10 +137,10 @@ class Stepper:
     def tune_key(self):
         cfg = self.cfg
         dev = torch.cuda.get_device_name()
-        return "%s|%s|nd%d|mesh%s|blk%s|%s|%s|%s|exact%d" % (
+        return "%s|%s|nd%d|mesh%s|blk%s|ng%d|nvar%d|%s|%s|%s|exact%d" % (
             dev, cfg.name, cfg.ndim, "x".join(map(str, cfg.mesh_nx)),
-            "x".join(map(str, cfg.block_nx)), cfg.recon, cfg.rsolver, cfg.integrator,
-            int(self.exact))
+            "x".join(map(str, cfg.block_nx)), cfg.ng, cfg.nvar, cfg.recon, cfg.rsolver,
+            cfg.integrator, int(self.exact))
 
     def autotune(self, trial_steps=2, cache=TUNE_CACHE, use_cache=True):
         """Pick the fastest launch configuration (cached per workload and GPU)."""

@@ -1,22 +1,36 @@
 """Passive scalars (hydro/composition; fluxes upwinded by the mass flux, hydro.cpp:607-615)
-on the per-kernel path: every step bit-identical to the oracle in exact mode, 1e-12 in fast
-mode, tracer mass conserved."""
+on the per-kernel path and the batched stepper: every step bit-identical to the oracle in
+exact mode, 1e-12 in fast mode, tracer mass conserved."""
 import numpy as np
 import pytest
 
 from apophis_gb300 import hydro, problems
+from apophis_gb300.stepper import Stepper
 from oracle import oracle as O
 from parity_util import assert_parity
 
 pytestmark = pytest.mark.gpu
 
+WORKLOADS = [
+    ("kh2d_plm_hllc", lambda: problems.kh2d_tracers(n=48, block=16, ng=2)),
+    ("kh2d_ppm_hlle", lambda: problems.kh2d_tracers(n=48, block=16, ng=3, recon="ppm", rsolver="hlle")),
+    ("kh2d_dc_hlle", lambda: problems.kh2d_tracers(n=48, block=16, ng=2, recon="dc", rsolver="hlle")),
+    ("kh3d_ppm_hllc", lambda: problems.with_tracers(*problems.kh3d(n=16, block=8, ng=4), nscalars=3)),
+    ("sod_plm_lhllc", lambda: problems.with_tracers(*problems.sod(nx=128, rsolver="lhllc", block_nx=32), nscalars=1)),
+]
+IDS = [w[0] for w in WORKLOADS]
 
-@pytest.mark.parametrize("recon,rsolver", [("plm", "hllc"), ("ppm", "hlle"), ("dc", "hlle")])
+
+def _interior(cfg, a):
+    sk, sj, si = cfg.interior
+    return a[:, :, sk, sj, si]
+
+
 @pytest.mark.parametrize("per_block", [False, True], ids=["per_pack", "per_block"])
-def test_scalars_match_oracle(cuda, recon, rsolver, per_block):
-    ng = 3 if recon == "ppm" else 2
-    cfg, cons = problems.kh2d_tracers(n=48, block=16, ng=ng, recon=recon, rsolver=rsolver)
-    assert cfg.nvar == 7
+@pytest.mark.parametrize("wl", WORKLOADS, ids=IDS)
+def test_scalars_per_kernel_match_oracle(cuda, wl, per_block):
+    cfg, cons = wl[1]()
+    assert cfg.nvar > 5
     for exact in (True, False):
         nsteps = 3 if exact else 1
         m = O.Mesh(cfg)
@@ -24,22 +38,72 @@ def test_scalars_match_oracle(cuda, recon, rsolver, per_block):
         m.run(nsteps=nsteps)
         d = hydro.Driver(cfg, cons, exact=exact, per_block=per_block)
         d.run(nsteps=nsteps)
-        assert d.time == m.state()["time"] or not exact
-        sk, sj, si = cfg.interior
-        got = d.cons()[:, :, sk, sj, si]
-        want = m.get("cons")[:, :, sk, sj, si]
-        assert_parity(got, want, exact, what="cons")
+        if exact:
+            assert d.time == m.state()["time"]
+        assert_parity(_interior(cfg, d.cons()), _interior(cfg, m.get("cons")), exact, what="cons")
         d.md.close()
+
+
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+@pytest.mark.parametrize("wl", WORKLOADS, ids=IDS)
+def test_scalars_stepper_match_oracle(cuda, wl, exact):
+    cfg, cons = wl[1]()
+    m = O.Mesh(cfg)
+    m.set_cons(cons)
+    st = Stepper(cfg, cons, exact=exact)
+    for _ in range(3 if exact else 1):
+        m.run(nsteps=1)
+        st.step(1)
+        if exact:
+            assert st.status()["dt"] == m.state()["dt"]
+        assert_parity(_interior(cfg, st.state()), _interior(cfg, m.get("cons")), exact, what="cons")
+    st.close()
+
+
+@pytest.mark.parametrize("make,lines", [
+    (lambda: problems.with_tracers(*problems.kh3d(n=16, block=8, ng=4), nscalars=2), [6, 6, 6]),
+    (lambda: problems.kh2d_tracers(n=64, block=32, ng=4, recon="ppm", rsolver="hllc"), [6, 6, 0]),
+])
+def test_scalars_tma_windows_match_plain_loads(cuda, make, lines):
+    """TMA windows carrying nvar > 5 variables: bit-identical to plain loads."""
+    cfg, cons = make()
+    outs = []
+    for tma in (0, 1):
+        st = Stepper(cfg, cons, exact=False)
+        c = st.config
+        c.update(lines=lines, tma=tma, schedule=2)
+        st.set_config(c)
+        st.step(3)
+        outs.append((st.state(), st.status()))
+        st.close()
+    assert np.array_equal(outs[1][0], outs[0][0]) and outs[1][1] == outs[0][1]
+
+
+def test_scalars_stepper_autotune_and_conservation(cuda):
+    cfg, cons = problems.with_tracers(*problems.kh3d(n=32, block=16, ng=4), nscalars=2)
+    st = Stepper(cfg, cons, exact=False)
+    st.autotune(trial_steps=2)
+    st.step(10)
+    out = _interior(cfg, st.state())
+    for k in range(cfg.nscalars):
+        before = _interior(cfg, cons)[:, 5 + k].sum()
+        assert abs(out[:, 5 + k].sum() - before) <= 1e-12 * abs(before)
+    st.close()
 
 
 def test_tracer_mass_conserved(cuda):
     cfg, cons = problems.kh2d_tracers(n=64, block=32, ng=2)
     d = hydro.Driver(cfg, cons, exact=False)
     d.run(nsteps=20)
-    sk, sj, si = cfg.interior
-    out = d.cons()
+    out = _interior(cfg, d.cons())
     for k in range(cfg.nscalars):
-        before = cons[:, 5 + k][:, sk, sj, si].sum()
-        after = out[:, 5 + k][:, sk, sj, si].sum()
-        assert abs(after - before) <= 1e-12 * abs(before)
+        before = _interior(cfg, cons)[:, 5 + k].sum()
+        assert abs(out[:, 5 + k].sum() - before) <= 1e-12 * abs(before)
     d.md.close()
+
+
+def test_scalars_rejected_where_not_carried(cuda):
+    from apophis_gb300 import adjoint
+    cfg, cons = problems.kh2d_tracers(n=32, block=16, ng=2)
+    with pytest.raises(Exception, match="passive scalars"):
+        adjoint.Adjoint(cfg)
