@@ -43,7 +43,7 @@ __device__ __forceinline__ const BLK &amr_fine_nbr(const BLK *blocks, const BLK 
 }
 
 // Ghost value (5 components) of face (d, s) of block B at depth k, transverse index t, for
-// the state returned by q(block).
+// the state q(block, component, cell).
 template <class BLK, class Q>
 __device__ void amr_ghost(const BLK *blocks, const BLK &B, Q q, const int (*bc)[2], int ng,
                           int d, int s, int k, int t, double *out) {
@@ -53,21 +53,19 @@ __device__ void amr_ghost(const BLK *blocks, const BLK &B, Q q, const int (*bc)[
     const BLK &N = blocks[B.amr.nbr[face][0]];
     const int a = s == 0 ? N.nx[d] - 1 - k : k;
     const int tn = B.amr.origin[td] + t - N.amr.origin[td];
-    const double *qn = q(N);
     const long long c = amr_cell(N, ng, d, a, tn);
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v) out[v] = qn[v * N.ncell + c];
+    for (int v = 0; v < NHYDRO; ++v) out[v] = q(N, v, c);
   } else if (kind == FACE_BOUNDARY) {
-    const double *qb = q(B);
     if (bc[d][s] == 1) {  // outflow
       const long long c = amr_cell(B, ng, d, s == 0 ? 0 : B.nx[d] - 1, t);
 #pragma unroll
-      for (int v = 0; v < NHYDRO; ++v) out[v] = qb[v * B.ncell + c];
+      for (int v = 0; v < NHYDRO; ++v) out[v] = q(B, v, c);
     } else {              // reflecting
       const long long c = amr_cell(B, ng, d, s == 0 ? k : B.nx[d] - 1 - k, t);
 #pragma unroll
       for (int v = 0; v < NHYDRO; ++v) {
-        const double x = qb[v * B.ncell + c];
+        const double x = q(B, v, c);
         out[v] = (v == 1 + d) ? -x : x;
       }
     }
@@ -77,14 +75,11 @@ __device__ void amr_ghost(const BLK *blocks, const BLK &B, Q q, const int (*bc)[
     const int ft = tg2 - F.amr.origin[td];
     const int a0 = s == 0 ? F.nx[d] - 1 - 2 * k : 2 * k;
     const int a1 = s == 0 ? a0 - 1 : a0 + 1;
-    const double *qf = q(F);
     const long long c00 = amr_cell(F, ng, d, a0, ft), c01 = amr_cell(F, ng, d, a0, ft + 1);
     const long long c10 = amr_cell(F, ng, d, a1, ft), c11 = amr_cell(F, ng, d, a1, ft + 1);
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v) {
-      const double *p = qf + v * F.ncell;
-      out[v] = ((p[c00] + p[c01]) + (p[c10] + p[c11])) * 0.25;
-    }
+    for (int v = 0; v < NHYDRO; ++v)
+      out[v] = ((q(F, v, c00) + q(F, v, c01)) + (q(F, v, c10) + q(F, v, c11))) * 0.25;
   } else {  // coarser neighbour: prolongation
     const BLK &C = blocks[B.amr.nbr[face][0]];
     const int tg = B.amr.origin[td] + t;
@@ -95,39 +90,36 @@ __device__ void amr_ghost(const BLK *blocks, const BLK &B, Q q, const int (*bc)[
     const double on = (gf & 1) ? 0.25 : -0.25;
     const double ot = (tg & 1) ? 0.25 : -0.25;
     const int tf0 = 2 * (tc + C.amr.origin[td]) - B.amr.origin[td];
-    const double *qc = q(C);
-    const double *qb = q(B);
     const bool has_t = tc - 1 >= 0 && tc + 1 < C.nx[td];
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) {
-      const double *pc = qc + v * C.ncell;
-      const double *pb = qb + v * B.ncell;
-      const double c = pc[amr_cell(C, ng, d, ic, tc)];
+      auto pc = [&](int a, int tt) { return q(C, v, amr_cell(C, ng, d, a, tt)); };
+      auto pb = [&](int a, int tt) { return q(B, v, amr_cell(B, ng, d, a, tt)); };
+      const double c = pc(ic, tc);
       auto restricted = [&](int a0, int a1) {
-        return ((pb[amr_cell(B, ng, d, a0, tf0)] + pb[amr_cell(B, ng, d, a0, tf0 + 1)]) +
-                (pb[amr_cell(B, ng, d, a1, tf0)] + pb[amr_cell(B, ng, d, a1, tf0 + 1)])) * 0.25;
+        return ((pb(a0, tf0) + pb(a0, tf0 + 1)) + (pb(a1, tf0) + pb(a1, tf0 + 1))) * 0.25;
       };
       double cm, cp;
       if (s == 0) {
-        cm = pc[amr_cell(C, ng, d, ic - 1, tc)];
-        cp = ic + 1 < C.nx[d] ? pc[amr_cell(C, ng, d, ic + 1, tc)] : restricted(0, 1);
+        cm = pc(ic - 1, tc);
+        cp = ic + 1 < C.nx[d] ? pc(ic + 1, tc) : restricted(0, 1);
       } else {
-        cm = ic - 1 >= 0 ? pc[amr_cell(C, ng, d, ic - 1, tc)] : restricted(B.nx[d] - 1, B.nx[d] - 2);
-        cp = pc[amr_cell(C, ng, d, ic + 1, tc)];
+        cm = ic - 1 >= 0 ? pc(ic - 1, tc) : restricted(B.nx[d] - 1, B.nx[d] - 2);
+        cp = pc(ic + 1, tc);
       }
       const double sn = amr_minmod(c - cm, cp - c);
       double st = 0.0;
-      if (has_t)
-        st = amr_minmod(c - pc[amr_cell(C, ng, d, ic, tc - 1)], pc[amr_cell(C, ng, d, ic, tc + 1)] - c);
+      if (has_t) st = amr_minmod(c - pc(ic, tc - 1), pc(ic, tc + 1) - c);
       out[v] = c + on * sn + ot * st;
     }
   }
 }
 
-// Fill the ghost cell c (entire-domain index) of block B.
+// Fill the ghost cell c (entire-domain index) of block B's field dst (nvar x ncell) from
+// the state q(block, component, cell).
 template <class BLK, class Q>
-__device__ void amr_fill_cell(const BLK *blocks, const BLK &B, Q q, const int (*bc)[2], int ng,
-                              long long c) {
+__device__ void amr_fill_cell(const BLK *blocks, const BLK &B, Q q, double *dst, const int (*bc)[2],
+                              int ng, long long c) {
   const int i = (int)(c % B.ni), j = (int)(c / B.ni);
   const bool gi = i < ng || i >= ng + B.nx[0];
   const bool gj = j < ng || j >= ng + B.nx[1];
@@ -136,9 +128,8 @@ __device__ void amr_fill_cell(const BLK *blocks, const BLK &B, Q q, const int (*
   if (gi && gj) {
     const int ci = min(max(i, ng), ng + B.nx[0] - 1);
     const int cj = min(max(j, ng), ng + B.nx[1] - 1);
-    const double *qb = q(B);
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v) val[v] = qb[v * B.ncell + (long long)cj * B.ni + ci];
+    for (int v = 0; v < NHYDRO; ++v) val[v] = q(B, v, (long long)cj * B.ni + ci);
   } else if (gi) {
     const int s = i < ng ? 0 : 1;
     amr_ghost(blocks, B, q, bc, ng, 0, s, s == 0 ? ng - 1 - i : i - (ng + B.nx[0]), j - ng, val);
@@ -146,9 +137,8 @@ __device__ void amr_fill_cell(const BLK *blocks, const BLK &B, Q q, const int (*
     const int s = j < ng ? 0 : 1;
     amr_ghost(blocks, B, q, bc, ng, 1, s, s == 0 ? ng - 1 - j : j - (ng + B.nx[1]), i - ng, val);
   }
-  double *qw = const_cast<double *>(q(B));
 #pragma unroll
-  for (int v = 0; v < NHYDRO; ++v) qw[v * B.ncell + c] = val[v];
+  for (int v = 0; v < NHYDRO; ++v) dst[v * B.ncell + c] = val[v];
 }
 
 }  // namespace aph

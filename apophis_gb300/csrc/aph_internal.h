@@ -55,6 +55,9 @@ struct PackDev {
 // (entire domain) and the accumulated flux difference du (interior only).
 struct StepBlock {
   double *u0, *u1, *prim, *gamma, *du;
+  // total energy of each cell before and after the floors of the last step's end (efl: the
+  // all-ones NaN where no floor changed it), so that the next ConsToPrim floors once
+  double *eraw, *efl;
   double *bflux;      // refined meshes: fluxes of the 4 boundary faces, [face][t][5]
   int member;         // ensembles: the member (independent problem) the block belongs to
   int nx[3];

@@ -38,6 +38,11 @@ __global__ void __launch_bounds__(kThreads) k_cons_to_prim(PackDev p, const Bloc
 #pragma unroll
   for (int n = 0; n < NHYDRO; ++n) B.prim[n * nc + c] = w[n];
   if (B.gamma) {
+#if !APH_EXACT
+    // the flux kernels reconstruct these fields: the reference's values, not the constants
+    // the fast ConsToPrim leaves where no floor fired
+    if (!fl) gamma_ref(u, p.gm1, g_c, g_e);
+#endif
     B.gamma[c] = g_c;
     B.gamma[nc + c] = g_e;
   }

@@ -90,6 +90,38 @@ __device__ __forceinline__ double eos_bulk_modulus(double gm1, double rho, doubl
   return lt(small, b) ? b : small;
 }
 
+// The reference's ConsToPrim arithmetic after the density floor (hydro.cpp:502-531), one
+// rounded operation at a time in its order: the fast build contracts products and sums into
+// FMAs, and these values must match the reference bit for bit where they feed the
+// discontinuous PPM limiters (the adiabatic-index fields of blocks where a floor fired, which
+// the fast mode otherwise replaces by the constants) or the non-idempotent pressure floor.
+// u_d: the floored density, di = 1 / u_d.  Sets u[IEN], w[IPR], g_c, g_e; returns whether
+// the pressure floor fired.
+__device__ __forceinline__ bool cons_to_prim_tail(double *u, double *w, double &g_c, double &g_e,
+                                                  double u_d, double di, double gm1, double pfloor) {
+  const double m1 = u[IM1], m2 = u[IM2], m3 = u[IM3];
+  const double e_k = __dmul_rn(__dmul_rn(0.5, di),
+                               __dadd_rn(__dadd_rn(__dmul_rn(m1, m1), __dmul_rn(m2, m2)), __dmul_rn(m3, m3)));
+  double u_e = u[IEN];
+  double w_p = __dmul_rn(__dmul_rn(gm1, u_d), __ddiv_rn(__dsub_rn(u_e, e_k), u_d));
+  w_p = is_neg(w_p) ? 0.0 : w_p;  // eos_pressure
+  const bool floored = !gt(w_p, pfloor);
+  if (floored) {
+    const double gm1q = __ddiv_rn(w_p, __dmul_rn(u_d, e_k));  // hydro.cpp:517
+    u_e = __dadd_rn(__ddiv_rn(pfloor, gm1q), e_k);
+    w_p = pfloor;
+  }
+  u[IEN] = u_e;
+  w[IPR] = w_p;
+  const double sie = __ddiv_rn(__dsub_rn(u_e, e_k), u_d);
+  const double small = 10.0 * 2.2250738585072014e-308;
+  double b = __dmul_rn(__dmul_rn(__dmul_rn(gm1, __dadd_rn(gm1, 1.0)), u_d), sie);  // eos_bulk_modulus
+  b = lt(small, b) ? b : small;
+  g_c = __ddiv_rn(b, w_p);
+  g_e = __dadd_rn(__ddiv_rn(w_p, __dsub_rn(u_e, e_k)), 1.0);
+  return floored;
+}
+
 // ConsToPrim for one cell (hydro.cpp:459-531, ideal gas).  u[] is updated in place
 // by the floors (density, energy); w[] gets rho, v1, v2, v3, p; g_c, g_e the two
 // adiabatic indices.  Returns true when the pressure floor was applied.
@@ -103,16 +135,14 @@ __device__ __forceinline__ bool cons_to_prim_cell(double *u, double *w, double &
   w[IV1] = u[IM1] * di;
   w[IV2] = u[IM2] * di;
   w[IV3] = u[IM3] * di;
-  const double e_k = 0.5 * di * (u[IM1] * u[IM1] + u[IM2] * u[IM2] + u[IM3] * u[IM3]);
-  double u_e = u[IEN];
 #if !APH_EXACT
   // fast: p = gm1 rho ((E - e_k) / rho) = gm1 (E - e_k), and with the floors inactive both
   // adiabatic indices are gamma (B / p = gm1 + 1 = p / (rho e) + 1), so one division per cell
   {
-    const double pe = gm1 * (u_e - e_k);
+    const double e_k = 0.5 * di * (u[IM1] * u[IM1] + u[IM2] * u[IM2] + u[IM3] * u[IM3]);
+    const double pe = gm1 * (u[IEN] - e_k);
     const double wp = is_neg(pe) ? 0.0 : pe;
     if (gt(wp, pfloor)) {
-      u[IEN] = u_e;
       w[IPR] = wp;
       g_c = gm1 + 1.0;
       g_e = g_c;
@@ -120,18 +150,14 @@ __device__ __forceinline__ bool cons_to_prim_cell(double *u, double *w, double &
     }
   }
 #endif
-  double w_p = eos_pressure(gm1, u_d, (u_e - e_k) / u_d);
-  const bool floored = !gt(w_p, pfloor);
-  if (floored) {
-    const double gm1q = w_p / (u_d * e_k);  // hydro.cpp:517
-    u_e = (pfloor / gm1q) + e_k;
-    w_p = pfloor;
-  }
-  u[IEN] = u_e;
-  w[IPR] = w_p;
-  g_c = eos_bulk_modulus(gm1, u_d, (u_e - e_k) / u_d) / w_p;
-  g_e = w_p / (u_e - e_k) + 1;
-  return floored;
+  return cons_to_prim_tail(u, w, g_c, g_e, u_d, di, gm1, pfloor);
+}
+
+// The reference's adiabatic indices (gamma_c, gamma_e) of a cell whose floors did not fire,
+// from its conserved state after ConsToPrim (u: the cell's five values).
+__device__ __forceinline__ void gamma_ref(const double *u, double gm1, double &g_c, double &g_e) {
+  double uu[NHYDRO] = {u[0], u[1], u[2], u[3], u[4]}, w[NHYDRO];
+  cons_to_prim_tail(uu, w, g_c, g_e, u[IDN], 1.0 / u[IDN], gm1, -1.0);
 }
 
 // ---- reconstruction (src/recon) --------------------------------------------------

@@ -173,6 +173,29 @@ __device__ __forceinline__ int map_index(int g, int n, int lo, int hi, bool &fli
   return g;
 }
 
+// ---- floors at step boundaries ----------------------------------------------------------
+// The reference applies the floors of ConsToPrim once to every new state, at the end of the
+// stage that made it (FillDerived), and its pressure floor is not idempotent: it rebuilds E
+// from the pressure before the floor (hydro.cpp:517-521).  Here a stage floors its input at
+// its start, and the last stage of a step also stores its output floored (what a caller then
+// reads is the reference's state) while keeping, per floored cell, the energy before the
+// floor (eraw) and after it (efl).  The first stage of the next step reads the energy before
+// the floor wherever the stored energy is still the floored one, so the floor is applied once.
+constexpr unsigned long long kNoFloorTag = ~0ULL;  // a NaN that arithmetic never produces
+
+__device__ __forceinline__ double energy_in(const StepBlock &X, long long c, bool step_start) {
+  const double e = X.u0[IEN * X.ncell + c];
+  if (!step_start) return e;
+  return __double_as_longlong(e) == __double_as_longlong(X.efl[c]) ? X.eraw[c] : e;
+}
+
+__device__ __forceinline__ void store_floored_energy(const StepBlock &X, long long c, double e_raw,
+                                                     double e_floored) {
+  const bool changed = __double_as_longlong(e_raw) != __double_as_longlong(e_floored);
+  X.efl[c] = changed ? e_floored : __longlong_as_double((long long)kNoFloorTag);
+  if (changed) X.eraw[c] = e_raw;
+}
+
 __device__ void ghost_cell(const StageArgs &a, const StepBlock &B, long long c) {
   const PackDev &p = a.p;
   const int idx[3] = {(int)(c % B.ni), (int)((c / B.ni) % B.nj), (int)(c / ((long long)B.ni * B.nj))};
@@ -196,7 +219,7 @@ __device__ void ghost_cell(const StageArgs &a, const StepBlock &B, long long c) 
   const long long sc = ((long long)si[2] * S.nj + si[1]) * S.ni + si[0];
 #pragma unroll
   for (int n = 0; n < NHYDRO; ++n) {
-    double v = S.u0[n * S.ncell + sc];
+    double v = n == IEN ? energy_in(S, sc, a.copy_u1) : S.u0[n * S.ncell + sc];
     if ((n == IM1 && flip[0]) || (n == IM2 && flip[1]) || (n == IM3 && flip[2])) v = -v;
     B.u0[n * B.ncell + c] = v;
   }
@@ -310,11 +333,27 @@ __host__ __device__ constexpr size_t pass_smem_doubles(int recon, int n, int T, 
              : (size_t)V * T * ((n + 2 * (recon == RECON_PLM ? 2 : 1)) + 2 * (n + 2));
 }
 
-// Doubles between the window region and the TMA staging area: the window (nvar + 2
-// variables) is padded to a multiple of 16 doubles so that the staging area starts 128-byte
-// aligned.
+// Reconstructed slabs beyond the nvar primitives that shared memory is sized for: the exact
+// build always reconstructs the two adiabatic-index fields; the fast build sizes for
+// constant-gamma items and splits an item of a block where a floor fired (which needs the
+// two extra slabs) into chunks of fewer lines (split_lines).
+#if APH_EXACT
+constexpr int kGammaSlabs = 2;
+#else
+constexpr int kGammaSlabs = 0;
+#endif
+
+// Lines of a chunk that fits the gamma slabs into the shared memory of T lines.
+__host__ __device__ constexpr int split_lines(int T, int nvar) {
+  return (nvar + kGammaSlabs) * T / (nvar + 2) > 1 ? (nvar + kGammaSlabs) * T / (nvar + 2) : 1;
+}
+
+// Doubles between the window region and the TMA staging area: the window (nvar +
+// kGammaSlabs variables) is padded to a multiple of 16 doubles so that the staging area
+// starts 128-byte aligned.
 __host__ __device__ constexpr size_t tma_stage_offset(int recon, int n, int T, int nvar) {
-  return ((size_t)(nvar + 2) * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1)) + 15) /
+  return ((size_t)(nvar + kGammaSlabs) * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1)) +
+          15) /
          16 * 16;
 }
 
@@ -393,8 +432,28 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
       if (DIR == 1) { t = r / NW; w = r - t * NW; } else { w = r / nl; t = r - w * nl; }
       long long base, stride, ib, is;
       line_of<DIR>(B, a.p.ndim, a.p.ng, l0 + t, base, stride, ib, is);
-      const double *src = v < nv ? B.prim + v * nc : B.gamma + (v - nv) * nc;
-      W[((size_t)v * T + t) * NW + w] = src[base + (long long)(w - G) * stride];
+      const long long cell = base + (long long)(w - G) * stride;
+      double x;
+      if (v < nv) {
+        x = B.prim[v * nc + cell];
+      } else {
+#if APH_EXACT
+        x = B.gamma[(v - nv) * nc + cell];
+#else
+        // the fast ConsToPrim leaves the constants where no floor fired; the reference's
+        // values (which the limiters see) are recomputed from the cell's state there
+        if (__double_as_longlong(B.prim[IPR * nc + cell]) == __double_as_longlong(a.p.pfloor)) {
+          x = B.gamma[(v - nv) * nc + cell];  // floored: the reference's values already
+        } else {
+          double uc[NHYDRO], g_c, g_e;
+#pragma unroll
+          for (int k = 0; k < NHYDRO; ++k) uc[k] = B.u0[k * nc + cell];
+          gamma_ref(uc, gc.gm1, g_c, g_e);
+          x = v == nv ? g_c : g_e;
+        }
+#endif
+      }
+      W[((size_t)v * T + t) * NW + w] = x;
     }
   }
   __syncthreads();
@@ -571,17 +630,19 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
           u[IEN] += de * rho * beta_dt;
         }
 #pragma unroll
-        for (int v = 0; v < NHYDRO; ++v) {
-          B.u0[v * nc + cell] = u[v];
+        for (int v = 0; v < NHYDRO; ++v)
           bad |= ((__double_as_longlong(u[v]) >> 52) & 0x7ff) == 0x7ff;  // NaN or inf
-        }
         if (bad) a.ctl->nonfinite = 1;
-        if (a.last) {  // EstimateTimestep on the floored new state
+        if (a.last) {  // EstimateTimestep on the floored new state, which is stored floored
           double w[NHYDRO], gcc, gce;
+          const double e_raw = u[IEN];
           const bool fl = cons_to_prim_cell(u, w, gcc, gce, gc.gm1, a.p.dfloor, a.p.pfloor);
           const unsigned long long b = dt_bits(dt_cell(w, u[IEN], B.dx, a.p.ndim, gc, fl));
           mymin = b < mymin ? b : mymin;
+          store_floored_energy(B, cell, e_raw, u[IEN]);
         }
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + cell] = u[v];
       }
       if (a.last) {
         if (a.members) member_min(a, B.member, mymin);
@@ -651,17 +712,19 @@ __device__ void amr_update(const StageArgs &a, const Sched &sched, unsigned int 
     }
     bool bad = false;
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v) {
-      B.u0[v * nc + c] = u[v];
+    for (int v = 0; v < NHYDRO; ++v)
       bad |= ((__double_as_longlong(u[v]) >> 52) & 0x7ff) == 0x7ff;  // NaN or inf
-    }
     if (bad) a.ctl->nonfinite = 1;
-    if (a.last) {
+    if (a.last) {  // dt of the floored new state, which is stored floored (as in pass_item)
       double wv[NHYDRO], gcc, gce;
+      const double e_raw = u[IEN];
       cons_to_prim_cell(u, wv, gcc, gce, p.gm1, p.dfloor, p.pfloor);
       const unsigned long long b = dt_bits(dt_candidate(wv, u[IEN], B.dx, p.ndim, p.gm1));
       dtmin = b < dtmin ? b : dtmin;
+      store_floored_energy(B, c, e_raw, u[IEN]);
     }
+#pragma unroll
+    for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + c] = u[v];
   }
 }
 
@@ -690,9 +753,15 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
     if (!active_of(a, B)) continue;
     const long long c = (long long)w.y + threadIdx.x;
     if (c < B.ncell) {
-      if (p.amr)
-        amr_fill_cell(a.blocks, B, [](const StepBlock &X) -> const double * { return X.u0; },
-                      p.bc, p.ng, c);
+      if (p.amr) {
+        const bool start = a.copy_u1;
+        amr_fill_cell(
+            a.blocks, B,
+            [start](const StepBlock &X, int v, long long i) {
+              return v == IEN ? energy_in(X, i, start) : X.u0[v * X.ncell + i];
+            },
+            B.u0, p.bc, p.ng, c);
+      }
       else
         ghost_cell(a, B, c);
     }
@@ -717,6 +786,7 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
         double u[NHYDRO], wv[NHYDRO], g_c, g_e;
 #pragma unroll
         for (int n = 0; n < NHYDRO; ++n) u[n] = B.u0[n * B.ncell + c];
+        u[IEN] = energy_in(B, c, true);  // the state of a step boundary
         cons_to_prim_cell(u, wv, g_c, g_e, gm1, p.dfloor, p.pfloor);
         cand = dt_bits(dt_candidate(wv, u[IEN], B.dx, p.ndim, gm1));
       }
@@ -730,6 +800,7 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
 #pragma unroll
     for (int n = 0; n < NHYDRO; ++n) u[n] = B.u0[n * nc + c];
     const double ud0 = u[IDN], ue0 = u[IEN];
+    u[IEN] = energy_in(B, c, a.copy_u1);
     const bool fl = cons_to_prim_cell(u, wv, g_c, g_e, gm1, p.dfloor, p.pfloor);
     int i, j, k;
     const bool inner = is_interior(p, B, c, i, j, k);
@@ -777,15 +848,20 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
 #else
       const bool constg = a.block_flags[w.x] == 0;
 #endif
-      if (dir == 1)
-        pass_item<1, RECON, RS>(a, B, w.x, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin, mbar,
-                                tma_phase);
-      else if (dir == 2)
-        pass_item<2, RECON, RS>(a, B, w.x, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin, mbar,
-                                tma_phase);
-      else
-        pass_item<3, RECON, RS>(a, B, w.x, w.y, nl, T, constg, first_pass, last_pass, sm, dtmin, mbar,
-                                tma_phase);
+      // the item's lines, in chunks that fit the gamma slabs where they are reconstructed
+      const int Tc = constg ? T : split_lines(T, p.nvar);
+      for (int o = 0; o < nl; o += Tc) {
+        const int l0 = w.y + o, nc = min(Tc, nl - o);
+        if (dir == 1)
+          pass_item<1, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin, mbar,
+                                  tma_phase);
+        else if (dir == 2)
+          pass_item<2, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin, mbar,
+                                  tma_phase);
+        else
+          pass_item<3, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin, mbar,
+                                  tma_phase);
+      }
     }
     if (!last_pass && !grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
   }
@@ -813,17 +889,24 @@ cudaError_t launch_barrier_probe(StepCtl *ctl, unsigned long long timeout_ns, cu
   return cudaGetLastError();
 }
 
+// Items of T lines with nvar + kGammaSlabs slabs, and single-line chunks with the gamma slabs
+// (split_lines never returns less than one line).
 size_t stage_smem_bytes(int recon, int n, int T, int nvar) {
-  return pass_smem_doubles(recon, n, T, nvar + 2) * sizeof(double);
+  const size_t a = pass_smem_doubles(recon, n, T, nvar + kGammaSlabs);
+  const size_t b = pass_smem_doubles(recon, n, 1, nvar + 2);
+  return (a > b ? a : b) * sizeof(double);
 }
 
 // With TMA staging: the window region padded to 128 bytes, then the larger of the remaining
 // pass regions and the staging area (nvar variables x T lines x the line's entire extent L).
 size_t stage_smem_bytes_tma(int recon, int n, int T, int L, int nvar) {
-  const size_t rest = pass_smem_doubles(recon, n, T, nvar + 2) -
-                      (size_t)(nvar + 2) * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1));
+  const int V = nvar + kGammaSlabs;
+  const size_t rest = pass_smem_doubles(recon, n, T, V) -
+                      (size_t)V * T * (n + 2 * (recon == RECON_PPM ? 3 : recon == RECON_PLM ? 2 : 1));
   const size_t stage = (size_t)2 * nvar * T * L;  // two boxes for items that cross a plane
-  return (tma_stage_offset(recon, n, T, nvar) + 16 + (rest > stage ? rest : stage)) * sizeof(double);
+  const size_t tma = (tma_stage_offset(recon, n, T, nvar) + 16 + (rest > stage ? rest : stage)) * sizeof(double);
+  const size_t plain = stage_smem_bytes(recon, n, T, nvar);
+  return tma > plain ? tma : plain;
 }
 
 template <int RECON, int MINB>

@@ -150,6 +150,7 @@ struct aph_stepper_s {
   std::vector<StepBlock> hblocks;
   StepBlock *d_blocks = nullptr;
   double *d_u1 = nullptr, *d_prim = nullptr, *d_gamma = nullptr, *d_du = nullptr;
+  double *d_eraw = nullptr, *d_efl = nullptr;  // energy before / after the step-end floors
   double *d_backup = nullptr;  // autotuner state backup
   int *d_flags = nullptr;
   StepCtl *d_ctl = nullptr;
@@ -261,31 +262,63 @@ aph_status encode_tmaps(aph_stepper s) {
   return e == cudaSuccess ? APH_OK : cuda_fail(e, "tensor maps");
 }
 
-// Build work lists, shared-memory size and grid for the current configuration.
-aph_status configure(aph_stepper s) {
-  destroy_graph(s);
+// Lines per item of every direction (requested counts, 0 = automatic, capped by the lines
+// of the largest block) and the shared memory a CTA needs for them.
+size_t stage_lines(aph_stepper s, const int lines[3], bool tma, int T_out[3]) {
   const PackDev &p = s->dev;
-  const int nb = p.nblocks;
   const int recon = s->params.recon;
-  // lines per item and shared memory per direction
   size_t smem = 0;
+  for (int d = 0; d < 3; ++d) T_out[d] = 0;
   for (int d = 0; d < p.ndim; ++d) {
     const int n = p.max_nx[d];
-    int T = s->cfg.lines[d] > 0 ? s->cfg.lines[d] : auto_lines(n);
+    int T = lines[d] > 0 ? lines[d] : auto_lines(n);
     int ntr_max = 1;
     for (const StepBlock &B : s->hblocks) {
       const int ntr = d == 0 ? B.nx[1] * B.nx[2] : d == 1 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1];
       ntr_max = std::max(ntr_max, ntr);
     }
     T = std::min(T, ntr_max);
-    s->T[d] = T;
+    T_out[d] = T;
     const int ext = d == 0 ? s->hblocks[0].ni : d == 1 ? s->hblocks[0].nj : s->hblocks[0].nk;
     const int nv = p.nvar;
-    const size_t need = s->cfg.tma ? (s->params.exact ? aph_exact::stage_smem_bytes_tma(recon, n, T, ext, nv)
-                                                      : aph_fast::stage_smem_bytes_tma(recon, n, T, ext, nv))
-                                   : (s->params.exact ? aph_exact::stage_smem_bytes(recon, n, T, nv)
-                                                      : aph_fast::stage_smem_bytes(recon, n, T, nv));
+    const size_t need = tma ? (s->params.exact ? aph_exact::stage_smem_bytes_tma(recon, n, T, ext, nv)
+                                               : aph_fast::stage_smem_bytes_tma(recon, n, T, ext, nv))
+                            : (s->params.exact ? aph_exact::stage_smem_bytes(recon, n, T, nv)
+                                               : aph_fast::stage_smem_bytes(recon, n, T, nv));
     smem = std::max(smem, need);
+  }
+  return smem;
+}
+
+// Resident stage CTAs per SM for a launch shape (the fewest over the kernels a step
+// launches: VL2's first stage reconstructs donor-cell); 0 if it does not fit.
+int stage_residency(aph_stepper s, int threads, int reg_cap, size_t smem) {
+  std::vector<int> recons = {s->params.recon};
+  if (s->integrator == APH_INTEGRATOR_VL2 && s->params.recon != APH_RECON_DC) recons.push_back(APH_RECON_DC);
+  int per_sm = 1 << 30;
+  for (int rc : recons) {
+    int k = 0;
+    cudaError_t e = s->params.exact
+                        ? aph_exact::stage_occupancy(rc, s->params.rsolver, threads, smem, reg_cap, &k)
+                        : aph_fast::stage_occupancy(rc, s->params.rsolver, threads, smem, reg_cap, &k);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    per_sm = std::min(per_sm, k);
+  }
+  return per_sm;
+}
+
+// Build work lists, shared-memory size and grid for the current configuration.
+aph_status configure(aph_stepper s) {
+  destroy_graph(s);
+  const PackDev &p = s->dev;
+  const int nb = p.nblocks;
+  // lines per item and shared memory per direction
+  const size_t smem = stage_lines(s, s->cfg.lines, s->cfg.tma != 0, s->T);
+  for (int d = 0; d < p.ndim; ++d) {
+    const int T = s->T[d];
     std::vector<int2> items;
     // schedule order: largest blocks first (longest-processing-time) so that the tail of a
     // pass holds the small items
@@ -311,18 +344,7 @@ aph_status configure(aph_stepper s) {
   }
   s->smem = smem;
   const int threads = s->cfg.threads;
-  // every kernel instance a step launches (vl2's first stage reconstructs donor-cell)
-  std::vector<int> recons = {recon};
-  if (s->integrator == APH_INTEGRATOR_VL2 && recon != APH_RECON_DC) recons.push_back(APH_RECON_DC);
-  int per_sm = 1 << 30;
-  for (int rc : recons) {
-    int k = 0;
-    cudaError_t e = s->params.exact
-                        ? aph_exact::stage_occupancy(rc, s->params.rsolver, threads, smem, s->cfg.reg_cap, &k)
-                        : aph_fast::stage_occupancy(rc, s->params.rsolver, threads, smem, s->cfg.reg_cap, &k);
-    if (e != cudaSuccess) return cuda_fail(e, "stage occupancy");
-    per_sm = std::min(per_sm, k);
-  }
+  int per_sm = stage_residency(s, threads, s->cfg.reg_cap, smem);
   if (per_sm < 1) return fail(APH_ERR_UNSUPPORTED, "stage kernel does not fit on an SM");
   if (s->cfg.ctas_per_sm > 0) per_sm = std::min(per_sm, s->cfg.ctas_per_sm);
   int dev = 0, sms = 0;
@@ -469,6 +491,8 @@ void free_all(aph_stepper s) {
   cudaFree(s->d_prim);
   cudaFree(s->d_gamma);
   cudaFree(s->d_du);
+  cudaFree(s->d_eraw);
+  cudaFree(s->d_efl);
   cudaFree(s->d_backup);
   cudaFree(s->d_flags);
   cudaFree(s->d_ctl);
@@ -514,9 +538,15 @@ __global__ void k_members_reset(MemberCtl *m, int n) {
 namespace aph {
 size_t stepper_field_doubles(aph_stepper s) { return (size_t)s->dev.nvar * s->total_cells; }
 
+// Forget the energies kept across the last step's floors: the state was replaced.
+cudaError_t forget_floors(aph_stepper s, cudaStream_t st) {
+  return cudaMemsetAsync(s->d_efl, 0xff, sizeof(double) * s->total_cells, st);
+}
+
 cudaError_t stepper_restart(aph_stepper s, cudaStream_t st) {
   k_ctl_init<<<1, 1, 0, st>>>(s->d_ctl, DBL_MAX, 0.0);
   cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = forget_floors(s, st);
   if (e == cudaSuccess && s->d_members) {
     k_members_reset<<<(s->nmembers + 127) / 128, 128, 0, st>>>(s->d_members, s->nmembers);
     e = cudaGetLastError();
@@ -717,6 +747,8 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   ck(cudaMalloc(&s->d_prim, sizeof(double) * nvar * cells));
   ck(cudaMalloc(&s->d_gamma, sizeof(double) * 2 * cells));
   ck(cudaMalloc(&s->d_du, sizeof(double) * nvar * inter));
+  ck(cudaMalloc(&s->d_eraw, sizeof(double) * cells));
+  ck(cudaMalloc(&s->d_efl, sizeof(double) * cells));
   ck(cudaMalloc(&s->d_flags, sizeof(int) * p.nblocks));
   ck(cudaMalloc(&s->d_ctl, sizeof(StepCtl)));
   ck(cudaMalloc(&s->d_blocks, sizeof(StepBlock) * p.nblocks));
@@ -755,12 +787,15 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
     B.prim = s->d_prim + (size_t)nvar * oc;
     B.gamma = s->d_gamma + 2 * oc;
     B.du = s->d_du + (size_t)nvar * oi;
+    B.eraw = s->d_eraw + oc;
+    B.efl = s->d_efl + oc;
     if (amr) B.bflux = s->d_bflux + (size_t)4 * s->bflux_stride * b;
     oc += B.ncell;
     oi += B.nint;
   }
   ck(cudaMemcpy(s->d_blocks, s->hblocks.data(), sizeof(StepBlock) * p.nblocks, cudaMemcpyHostToDevice));
   ck(cudaMemset(s->d_flags, 0, sizeof(int) * p.nblocks));
+  ck(cudaMemset(s->d_efl, 0xff, sizeof(double) * cells));
   k_ctl_init<<<1, 1>>>(s->d_ctl, desc->tlim > 0 ? desc->tlim : DBL_MAX, desc->fixed_dt);
   ck(cudaGetLastError());
   if (e != cudaSuccess) {
@@ -984,10 +1019,12 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
   // back up u0 of every block and the control block
   const int nv = s->dev.nvar;
   const size_t nbv = sizeof(double) * nv;
-  if (!s->d_backup) {
-    e = cudaMalloc(&s->d_backup, nbv * s->total_cells);
+  const size_t ncells = (size_t)s->total_cells;
+  if (!s->d_backup) {  // u0 of every block, then the energies kept across the step-end floors
+    e = cudaMalloc(&s->d_backup, (nbv + 2 * sizeof(double)) * ncells);
     if (e != cudaSuccess) return cuda_fail(e, "autotune backup");
   }
+  double *bk_eraw = s->d_backup + nv * ncells, *bk_efl = bk_eraw + ncells;
   StepCtl ctl_saved;
   e = cudaMemcpy(&ctl_saved, s->d_ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost);
   std::vector<MemberCtl> members_saved(s->nmembers);
@@ -999,6 +1036,8 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
     if (e == cudaSuccess) e = cudaMemcpy(s->d_backup + nv * off, B.u0, nbv * B.ncell, cudaMemcpyDeviceToDevice);
     off += B.ncell;
   }
+  if (e == cudaSuccess) e = cudaMemcpy(bk_eraw, s->d_eraw, sizeof(double) * ncells, cudaMemcpyDeviceToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(bk_efl, s->d_efl, sizeof(double) * ncells, cudaMemcpyDeviceToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "autotune backup");
   auto restore = [&]() {
     long long o = 0;
@@ -1006,99 +1045,31 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
       cudaMemcpy(B.u0, s->d_backup + nv * o, nbv * B.ncell, cudaMemcpyDeviceToDevice);
       o += B.ncell;
     }
+    cudaMemcpy(s->d_eraw, bk_eraw, sizeof(double) * ncells, cudaMemcpyDeviceToDevice);
+    cudaMemcpy(s->d_efl, bk_efl, sizeof(double) * ncells, cudaMemcpyDeviceToDevice);
     cudaMemcpy(s->d_ctl, &ctl_saved, sizeof(StepCtl), cudaMemcpyHostToDevice);
     if (s->nmembers)
       cudaMemcpy(s->d_members, members_saved.data(), sizeof(MemberCtl) * s->nmembers,
                  cudaMemcpyHostToDevice);
   };
-  // candidate set
-  std::vector<aph_stepper_config> cands;
   const aph_stepper_config base = s->cfg;
   const int ndim = s->dev.ndim;
-  std::vector<std::vector<int>> orders = {{1, 2, 3}};
-  if (!s->params.exact && ndim == 2) orders.push_back({2, 1, 3});
-  if (!s->params.exact && ndim == 3) {
-    orders.push_back({3, 2, 1});
-    orders.push_back({2, 3, 1});
-  }
-  for (int threads : {128, 256})
-    for (int lscale : {1, 2})
-      for (int sched : {0, 1, 2})
-        for (const auto &o : orders) {
-          aph_stepper_config c = base;
-          c.threads = threads;
-          c.schedule = sched;
-          c.ctas_per_sm = 0;
-          c.use_graph = 1;
-          for (int d = 0; d < 3; ++d) {
-            c.order[d] = o[d];
-            const int n = s->dev.max_nx[d];
-            const int auto_l = (n + 2 >= threads) ? 1 : std::max(1, threads / (n + 2));
-            c.lines[d] = std::max(1, auto_l * lscale);
-          }
-          cands.push_back(c);
-        }
-  double best_t = 1e300;
-  aph_stepper_config best_c = base;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  for (const aph_stepper_config &c : cands) {
-    if (aph_stepper_set_config(s, &c) != APH_OK) continue;
-    restore();
-    if (aph_stepper_step(s, 1, 0) != APH_OK) continue;  // warm-up (and graph build)
-    cudaEventRecord(e0, 0);
-    if (aph_stepper_step(s, trial_steps, 0) != APH_OK) continue;
-    cudaEventRecord(e1, 0);
-    cudaEventSynchronize(e1);
-    StepCtl c2;
-    if (read_ctl(s, &c2) != APH_OK) break;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    const double per = ms / trial_steps;
-    if (per < best_t) {
-      best_t = per;
-      best_c = c;
-    }
-  }
-  // second round: the register-capped kernel (three 256-thread CTAs per SM) with the best
-  // schedule and order, over the line counts
-  {
-    const aph_stepper_config b0 = best_c;
-    std::vector<aph_stepper_config> more;
-    for (int threads : {128, 256})
-      for (int lines : {0, 1, 2, 3}) {
-        aph_stepper_config c = b0;
-        c.reg_cap = 1;
-        c.threads = threads;
-        for (int d = 0; d < 3; ++d) {
-          const int n = s->dev.max_nx[d];
-          const int auto_l = (n + 2 >= threads) ? 1 : std::max(1, threads / (n + 2));
-          c.lines[d] = lines == 0 ? auto_l : lines == 1 ? 2 * auto_l : lines == 2 ? std::max(1, (7 * auto_l) / 3)
-                                                                                  : std::max(1, (5 * auto_l) / 3);
-        }
-        more.push_back(c);
-      }
-    // each with TMA-staged windows too, where the lines allow it (even, dividing a plane)
-    const size_t nmore = more.size();
-    for (size_t i = 0; i < nmore; ++i)
-      for (int rc : {0, 1}) {
-        aph_stepper_config c = more[i];
-        c.reg_cap = rc;
-        c.tma = 1;
-        for (int d = 0; d < 3; ++d) c.lines[d] = std::max(2, c.lines[d] - c.lines[d] % 2);
-        more.push_back(c);
-      }
-    for (const aph_stepper_config &c : more) {
+  double best_t = 1e300;
+  aph_stepper_config best_c = base;
+  auto trial = [&](const std::vector<aph_stepper_config> &cands) {
+    for (const aph_stepper_config &c : cands) {
       if (aph_stepper_set_config(s, &c) != APH_OK) continue;
       restore();
-      if (aph_stepper_step(s, 1, 0) != APH_OK) continue;
+      if (aph_stepper_step(s, 1, 0) != APH_OK) continue;  // warm-up (and graph build)
       cudaEventRecord(e0, 0);
       if (aph_stepper_step(s, trial_steps, 0) != APH_OK) continue;
       cudaEventRecord(e1, 0);
       cudaEventSynchronize(e1);
       StepCtl c2;
-      if (read_ctl(s, &c2) != APH_OK) break;
+      if (read_ctl(s, &c2) != APH_OK) return;
       float ms = 0;
       cudaEventElapsedTime(&ms, e0, e1);
       const double per = ms / trial_steps;
@@ -1107,6 +1078,90 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
         best_c = c;
       }
     }
+  };
+  // Launch shapes: for each CTA size, register budget and window staging, the line counts at
+  // the upper edge of each residency level (the most lines per item that still fit that many
+  // CTAs on an SM: more lines amortise a window's halo cells, more resident warps hide each
+  // other's barriers and loop tails), keeping levels of at least 8 warps per SM.
+  auto shapes = [&](int threads, int reg_cap, int tma, const aph_stepper_config &from) {
+    std::vector<aph_stepper_config> out;
+    int most = 1;
+    for (int d = 0; d < ndim; ++d)
+      for (const StepBlock &B : s->hblocks)
+        most = std::max(most, d == 0 ? B.nx[1] * B.nx[2] : d == 1 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1]);
+    most = std::min(most, 64);
+    int prev_occ = 0, prev_T = 0;
+    for (int T = tma ? 2 : 1; T <= most + 1; T += tma ? 2 : 1) {
+      int occ = 0;
+      if (T <= most) {
+        const int lines[3] = {T, T, T};
+        int Ts[3];
+        const size_t smem = stage_lines(s, lines, tma != 0, Ts);
+        if (smem <= 220 * 1024 && !(tma && tma_unsupported(s, Ts)))
+          occ = stage_residency(s, threads, reg_cap, smem);
+      }
+      if (occ != prev_occ && prev_occ > 0 && prev_occ * threads >= 256) {
+        aph_stepper_config c = from;
+        c.threads = threads;
+        c.reg_cap = reg_cap;
+        c.tma = tma;
+        c.ctas_per_sm = 0;
+        for (int d = 0; d < 3; ++d) c.lines[d] = d < ndim ? prev_T : 0;
+        out.push_back(c);
+      }
+      if (occ == 0 && prev_occ > 0) break;
+      prev_occ = occ;
+      prev_T = T;
+    }
+    return out;
+  };
+  // round 1: launch shapes with plain loads, strided schedule, x-y-z order
+  {
+    aph_stepper_config c0 = base;
+    c0.schedule = 0;
+    c0.use_graph = 1;
+    c0.tma = 0;
+    for (int d = 0; d < 3; ++d) c0.order[d] = d + 1;
+    std::vector<aph_stepper_config> cands;
+    for (int threads : {128, 256})
+      for (int rc : {0, 1}) {
+        const auto v = shapes(threads, rc, 0, c0);
+        cands.insert(cands.end(), v.begin(), v.end());
+      }
+    if (cands.empty()) cands.push_back(c0);
+    trial(cands);
+  }
+  // round 2: schedules and sweep orders (any order only in fast mode: exact mode keeps the
+  // reference's x, y, z summation) around the best shape
+  {
+    std::vector<std::vector<int>> orders = {{1, 2, 3}};
+    if (!s->params.exact && ndim == 2) orders.push_back({2, 1, 3});
+    if (!s->params.exact && ndim == 3) {
+      orders.push_back({3, 2, 1});
+      orders.push_back({2, 3, 1});
+    }
+    const aph_stepper_config b = best_c;
+    std::vector<aph_stepper_config> cands;
+    for (int sched : {0, 1, 2})
+      for (const auto &o : orders) {
+        aph_stepper_config c = b;
+        c.schedule = sched;
+        for (int d = 0; d < 3; ++d) c.order[d] = o[d];
+        if (sched != b.schedule || c.order[0] != b.order[0] || c.order[1] != b.order[1]) cands.push_back(c);
+      }
+    trial(cands);
+  }
+  // round 3: TMA-staged windows (even line counts) with the best schedule and order; fast
+  // mode only (exact mode reconstructs the gamma field, which the windows do not carry)
+  if (!s->params.exact) {
+    const aph_stepper_config b = best_c;
+    std::vector<aph_stepper_config> cands;
+    for (int threads : {128, 256})
+      for (int rc : {0, 1}) {
+        const auto v = shapes(threads, rc, 1, b);
+        cands.insert(cands.end(), v.begin(), v.end());
+      }
+    trial(cands);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -12,7 +12,7 @@ import math
 
 import numpy as np
 
-from .mesh import IDN, IEN, IM1, IM2, IM3, MeshConfig
+from .mesh import DEFAULT_FLOOR, IDN, IEN, IM1, IM2, IM3, MeshConfig
 
 
 def _alloc(cfg):
@@ -156,6 +156,27 @@ def blast2d(n=256, block=64, ng=4, r0=0.1, gamma=1.4, recon="ppm", rsolver="hllc
         r = np.sqrt((x - 0.5) ** 2 + (y - 0.5) ** 2)
         p = np.where(r < r0, p_in, p_out)
         _set_prim(cfg, cons, b, 1.0, 0.0, 0.0, 0.0, p)
+    return cfg, cons
+
+
+def rarefaction2d(n=48, block=16, ng=3, recon="ppm", rsolver="hllc", integrator="rk2", cfl=0.3,
+                  gamma=1.4, v0=3.0, pfloor=0.1, dfloor=None):
+    """Two-dimensional double rarefaction (Einfeldt's 1-2-3 problem, faster, turned 30 degrees
+    off the x axis): rho 1, p 0.4, the two halves moving apart at v0 along the normal of the
+    line through the centre, outflow boundaries.  The pressure between the two rarefactions
+    falls below the raised pressure floor (the reference's hydro/pfloor) from the fourth step
+    on, in the blocks along the line (5 of the 9 at the defaults) and in no other block."""
+    cfg = MeshConfig(ndim=2, mesh_nx=(n, n, 1), block_nx=(block, block, 1), ng=ng,
+                     recon=recon, rsolver=rsolver, integrator=integrator, cfl=cfl, gamma=gamma,
+                     bc=(("outflow", "outflow"), ("outflow", "outflow"), ("periodic", "periodic")),
+                     pfloor=pfloor, dfloor=dfloor if dfloor is not None else DEFAULT_FLOOR,
+                     name="rarefaction2d")
+    cons = _alloc(cfg)
+    nx_, ny_ = math.cos(math.pi / 6), math.sin(math.pi / 6)
+    for b in range(cfg.nblocks):
+        x, y, _ = cfg.cell_centers(b)
+        side = np.where((x - 0.5) * nx_ + (y - 0.5) * ny_ < 0.0, -1.0, 1.0)
+        _set_prim(cfg, cons, b, 1.0, side * v0 * nx_, side * v0 * ny_, 0.0, 0.4)
     return cfg, cons
 
 
