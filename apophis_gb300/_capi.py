@@ -125,6 +125,8 @@ SIGNATURES = {
                             ctypes.c_void_p], ctypes.c_int),
     "aph_hydro_history": ([ctypes.c_void_p, _dp, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_history": ([ctypes.c_void_p, _dp, ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_load_interiors": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_store_interiors": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_set_clock": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                ctypes.c_void_p], ctypes.c_int),
     "aph_diag_barrier_timeout": ([ctypes.c_double, ctypes.c_void_p], ctypes.c_int),

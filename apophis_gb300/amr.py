@@ -450,6 +450,9 @@ class AmrStepper(_StepperBase):
         self.h = ctypes.c_void_p()
         _capi.call("aph_stepper_create", ctypes.byref(desc), ctypes.byref(self.h))
 
+    def interior_values(self):
+        return 5 * self.cfg.zones()
+
     def tune_key(self):
         import torch
         cfg = self.cfg

@@ -64,6 +64,7 @@ struct StepBlock {
   int ni, nj, nk;
   int loc[3];
   long long ncell, nint;
+  long long ipre;     // interior cells of the blocks before this one (packed interiors)
   double dx[3];
   AmrFaces amr;
 };

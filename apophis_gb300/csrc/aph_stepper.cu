@@ -505,6 +505,29 @@ void free_all(aph_stepper s) {
   cudaFree(s->d_tmaps);
 }
 
+// Packed interiors <-> the state: grid.y = block; element e of a block's nvar * nint
+// interior values enumerates (var, k, j, i) in the packed order, so its packed index is
+// nvar * ipre + e.  Host memory is read or written directly (pinned, mapped).
+__global__ void k_interiors(const StepBlock *blocks, int ndim, int ng, int nvar, const double *src,
+                            double *dst, int load) {
+  const StepBlock &B = blocks[blockIdx.y];
+  const int n0 = B.nx[0], n1 = B.nx[1], n2 = B.nx[2];
+  const int sj = ndim >= 2 ? ng : 0, sk = ndim >= 3 ? ng : 0;
+  const long long total = (long long)nvar * B.nint;
+  const long long base = (long long)nvar * B.ipre;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long line = e / n0;
+    const int i = (int)(e - line * n0);
+    const int j = (int)(line % n1);
+    const long long kv = line / n1;
+    const int k = (int)(kv % n2), v = (int)(kv / n2);
+    const long long g = (long long)v * B.ncell + ((long long)(k + sk) * B.nj + (j + sj)) * B.ni + (i + ng);
+    if (load) B.u0[g] = src[base + e];
+    else dst[base + e] = B.u0[g];
+  }
+}
+
 __global__ void k_set_dt(StepCtl *c, MemberCtl *m, int n, const double *dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (!m) {
@@ -789,6 +812,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
     B.du = s->d_du + (size_t)nvar * oi;
     B.eraw = s->d_eraw + oc;
     B.efl = s->d_efl + oc;
+    B.ipre = oi;
     if (amr) B.bflux = s->d_bflux + (size_t)4 * s->bflux_stride * b;
     oc += B.ncell;
     oi += B.nint;
@@ -853,6 +877,66 @@ aph_status aph_stepper_step(aph_stepper s, int nsteps, void *stream) {
     if (e != cudaSuccess) return cuda_fail(e, "stage launch");
   }
   return APH_OK;
+}
+
+static aph_status interiors(aph_stepper s, const double *src, double *dst, bool load, void *stream) {
+  clear_error();
+  if (!s || !(load ? (const void *)src : (const void *)dst)) return fail(APH_ERR_INVALID, "NULL argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const void *ptr = load ? (const void *)src : (const void *)dst;
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, ptr);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    at.type = cudaMemoryTypeUnregistered;
+  }
+  const PackDev &p = s->dev;
+  const int nv = p.nvar;
+  if (at.type != cudaMemoryTypeUnregistered) {  // device, managed or pinned host memory
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (p.nblocks > 65535) return fail(APH_ERR_UNSUPPORTED, "more than 65535 blocks");
+    const dim3 grid(std::max(1, (4 * sms + p.nblocks - 1) / p.nblocks), p.nblocks);
+    k_interiors<<<grid, 256, 0, st>>>(s->d_blocks, p.ndim, p.ng, nv, src, dst, load ? 1 : 0);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? APH_OK : cuda_fail(e, "interiors");
+  }
+  // pageable host memory: one 3D copy per block and variable
+  for (const StepBlock &B : s->hblocks) {
+    const int sj = p.ndim >= 2 ? p.ng : 0, sk = p.ndim >= 3 ? p.ng : 0;
+    for (int v = 0; v < nv && e == cudaSuccess; ++v) {
+      double *packed = const_cast<double *>(load ? src : dst) + (size_t)nv * B.ipre + (size_t)v * B.nint;
+      double *state = B.u0 + (size_t)v * B.ncell;
+      cudaMemcpy3DParms c;
+      std::memset(&c, 0, sizeof(c));
+      const cudaPitchedPtr pk = make_cudaPitchedPtr(packed, sizeof(double) * B.nx[0], B.nx[0], B.nx[1]);
+      const cudaPitchedPtr sp = make_cudaPitchedPtr(state, sizeof(double) * B.ni, B.ni, B.nj);
+      const cudaPos at_state = make_cudaPos(sizeof(double) * p.ng, sj, sk);
+      c.extent = make_cudaExtent(sizeof(double) * B.nx[0], B.nx[1], B.nx[2]);
+      if (load) {
+        c.srcPtr = pk;
+        c.dstPtr = sp;
+        c.dstPos = at_state;
+        c.kind = cudaMemcpyHostToDevice;
+      } else {
+        c.srcPtr = sp;
+        c.srcPos = at_state;
+        c.dstPtr = pk;
+        c.kind = cudaMemcpyDeviceToHost;
+      }
+      e = cudaMemcpy3DAsync(&c, st);
+    }
+  }
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "interiors");
+}
+
+aph_status aph_stepper_load_interiors(aph_stepper s, const double *src, void *stream) {
+  return interiors(s, src, nullptr, true, stream);
+}
+
+aph_status aph_stepper_store_interiors(aph_stepper s, double *dst, void *stream) {
+  return interiors(s, nullptr, dst, false, stream);
 }
 
 aph_status aph_stepper_status(aph_stepper s, double *time, double *dt, int *ncycle, void *stream) {

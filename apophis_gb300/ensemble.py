@@ -109,6 +109,9 @@ class EnsembleStepper(_StepperBase):
     """All members in one stepper: one persistent launch per stage over every block, each
     member with its own gas constants, dt and clock (finished members are skipped)."""
 
+    def interior_values(self):
+        return 5 * sum(c.zones() for c in self.ens.members)
+
     def __init__(self, ens: Ensemble, cons0, exact=False, fixed_dt=0.0):
         import torch
         from . import _capi

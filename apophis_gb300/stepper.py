@@ -99,6 +99,34 @@ class Stepper:
                    int(d.NCycle), stream_handle())
         return st
 
+    def interior_shape(self):
+        """Shape of the packed interiors: (nblocks, nvar, nx3, nx2, nx1)."""
+        c = self.cfg
+        return (c.nblocks, c.nvar, c.block_nx[2], c.block_nx[1], c.block_nx[0])
+
+    def interior_values(self):
+        """Length of the packed interiors (every block's nvar x interior cells)."""
+        return self.cfg.nvar * self.cfg.zones()
+
+    def _packed(self, a):
+        n = self.interior_values()
+        if isinstance(a, torch.Tensor):
+            if a.dtype != torch.float64 or not a.is_contiguous() or a.numel() != n:
+                raise ValueError("packed interiors: a contiguous float64 tensor of %d values" % n)
+            return a.data_ptr()
+        if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.size != n:
+            raise ValueError("packed interiors: a C-contiguous float64 array of %d values" % n)
+        return a.ctypes.data
+
+    def load_interiors(self, src, stream=None):
+        """Replace the state's interiors with the packed array src (interior_shape; device,
+        pinned host or other host memory; asynchronous on the stream)."""
+        _capi.call("aph_stepper_load_interiors", self.h, self._packed(src), stream_handle(stream))
+
+    def store_interiors(self, dst, stream=None):
+        """Write the state's interiors into the packed array dst (interior_shape)."""
+        _capi.call("aph_stepper_store_interiors", self.h, self._packed(dst), stream_handle(stream))
+
     def history(self, stream=None):
         """GlobalQuantHst of the state: {"total_mass", "total_energy"}."""
         out = (ctypes.c_double * 2)()

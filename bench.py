@@ -7,8 +7,10 @@ whole pack (2 stages + the CFL dt reduction).
 
 value   zone-updates/s of the batched path (one persistent launch per stage over all 64
         meshblocks, the step replayed as a CUDA graph), state resident in HBM.
-e2e     the same through the C ABI with the state in pinned host memory: every step
-        copies cons host->device, steps, copies cons device->host.
+e2e     the same through the C ABI with the state in pinned host memory as the packed
+        interiors (aph_stepper_load_interiors / _store_interiors, one kernel each way across
+        the host link): every step loads its input from the host, steps, and stores its
+        result back to the host.
 plain   the per-meshblock launch path (one launch per kernel per meshblock).
 roofline  HBM roofline of the stage kernel with the algorithmic 200 B per zone-update
         (stage 1: read U^n, write U^1; stage 2: read U^1 and U^n, write U^n+1), and the
@@ -82,7 +84,8 @@ class ClockSampler:
     def __init__(self, gpu_index=0):
         self.gpu = gpu_index
         self.proc = None
-        self.path = "/tmp/aph_clocks_%d.csv" % os.getpid()
+        ClockSampler.count = getattr(ClockSampler, "count", 0) + 1
+        self.path = "/tmp/aph_clocks_%d_%d.csv" % (os.getpid(), ClockSampler.count)
 
     def __enter__(self):
         try:
@@ -528,19 +531,40 @@ def main():
     value = zones * ws / (ms * 1e-3)
     launches_per_step = 3  # two stage kernels + the dt-policy kernel
 
-    # e2e: host buffers through the C ABI, copies inside the timed region
-    host = torch.empty(st.cons.shape, dtype=torch.float64, pin_memory=True)
-    host.copy_(st.cons)
+    # e2e: the state in pinned host memory as the packed interiors, through the C ABI
+    # (aph_stepper_load_interiors / _store_interiors): every step loads its input from the
+    # host and stores its result back, inside the timed region
+    host = torch.empty(st.interior_shape(), dtype=torch.float64, pin_memory=True)
+    st.store_interiors(host)
     nbytes = host.numel() * 8
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        st.cons.copy_(host, non_blocking=True)
+
+    def e2e_step():
+        st.load_interiors(host)
         st.step(1)
-        host.copy_(st.cons, non_blocking=True)
-    barrier()
+        st.store_interiors(host)
+
+    for _ in range(max(1, min(args.warmup, 2))):  # first transfers of a fresh pinned buffer
+        e2e_step()
+    with ClockSampler(local) as clk_e2e:
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        barrier()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     e2e_value = zones * ws / (e2e_ms * 1e-3)
+    # the host link's share of an e2e step: the load and the store alone (CUDA events)
+    link = {}
+    for name, fn in (("load", lambda: st.load_interiors(host)), ("store", lambda: st.store_interiors(host))):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(3):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b) / 3
+        link[name + "_ms"] = t
+        link[name + "_gbs"] = nbytes / (t * 1e-3) / 1e9
     st.close()
     del st
     torch.cuda.empty_cache()
@@ -591,7 +615,8 @@ def main():
                    "l2": "no flush: inputs larger than L2 (state 1.0 GB, ~4 GB working set)",
                    "launch": tune["config"] if tune else None},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes},
+                "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "host_link": link,
+                "clocks": clk_e2e.summary()},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm,

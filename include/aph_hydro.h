@@ -255,6 +255,16 @@ aph_status aph_stepper_set_clock(aph_stepper stepper, double time, double dt, in
                                  void *stream);
 /* The history sums of the stepper's state (as aph_hydro_history, over all blocks). */
 aph_status aph_stepper_history(aph_stepper stepper, double out[2], void *stream);
+/* The interiors of the stepper's state as one packed array: block after block, each block's
+ * (nvar, nx3, nx2, nx1) interior cells (no ghost cells: a step refills them).  The array may
+ * be device memory or pinned host memory (cudaHostAlloc / cudaHostRegister), which one kernel
+ * reads or writes across the host link directly; other host memory is copied with one 3D copy
+ * per block and variable.  Asynchronous on stream.  No counterpart in the reference, whose
+ * state stays in Parthenon's per-block arrays; this is the host interface of a resident pack
+ * (a host code that keeps its state in host memory loads it before and stores it after each
+ * step or run). */
+aph_status aph_stepper_load_interiors(aph_stepper stepper, const double *src, void *stream);
+aph_status aph_stepper_store_interiors(aph_stepper stepper, double *dst, void *stream);
 aph_status aph_stepper_get_config(aph_stepper stepper, aph_stepper_config *cfg);
 aph_status aph_stepper_set_config(aph_stepper stepper, const aph_stepper_config *cfg);
 /* Advance nsteps steps without the graph, timing each stage launch with CUDA events on
