@@ -75,11 +75,9 @@ __device__ __forceinline__ double ppm_face_code(double qm1, double q0, double dd
                                                 double d2m1, double d20, int &code) {
   const double avg = 0.5 * (qm1 + q0);
   double dph = fma(ddm1 - dd0, 1.0 / 6.0, avg);
-  const double qa_tmp = dph - qm1;
-  const double qb_tmp = q0 - dph;
   const double qa = 3.0 * (qm1 + q0 - 2.0 * dph);
   code = PF_OPEN;
-  if (is_neg(qa_tmp * qb_tmp)) {
+  if (strictly_outside(dph, qm1, q0)) {  // the forward's test (ppm_face, fast mode)
     double qd = 0.0;
     code = PF_AVG;
     const bool sa = is_neg(qa);
@@ -127,11 +125,9 @@ __device__ __forceinline__ void ppm_cell_code(double q_im2, double q_im1, double
   ql = dph_hi;
   const double dqf_minus = q_i - qr;
   const double dqf_plus = ql - q_i;
-  const double qa_tmp = dqf_minus * dqf_plus;
-  const double qb_tmp = (q_ip1 - q_i) * (q_i - q_im1);
   code = 0;
   rho = 0.0;
-  if (!is_pos(qa_tmp) || !is_pos(qb_tmp)) {
+  if (!strictly_between(qr, q_i, ql) || !strictly_between(q_im1, q_i, q_ip1)) {  // as ppm_cell
     code = 1;
     double qe = 0.0;
     int src = 0;

@@ -69,6 +69,19 @@ __device__ __forceinline__ double flip_if(double v, bool neg) {
   return neg ? __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ULL) : v;
 }
 __device__ __forceinline__ double from_bits(unsigned long long b) { return __longlong_as_double((long long)b); }
+// b strictly between a and c: the reference's sign test (b - a) * (c - b) > 0 without the FP64
+// subtractions and product (a difference of finite doubles is zero only when they are
+// equal; the two differ only where the product underflows to zero, for differences of
+// order 1e-162).  Fast mode.
+__device__ __forceinline__ bool strictly_between(double a, double b, double c) {
+  const long long ka = okey(a), kb = okey(b), kc = okey(c);
+  return (ka < kb && kb < kc) || (ka > kb && kb > kc);
+}
+// x beyond both a and b on the same side: the sign test (x - a) * (b - x) < 0.  Fast mode.
+__device__ __forceinline__ bool strictly_outside(double x, double a, double b) {
+  const long long kx = okey(x), ka = okey(a), kb = okey(b);
+  return (kx > ka && kx > kb) || (kx < ka && kx < kb);
+}
 
 // ---- gamma-dependent constants of a pack (fast mode) ---------------------------
 struct GasConsts {
@@ -181,7 +194,11 @@ __device__ __forceinline__ void plm(double q_im1, double q_i, double q_ip1, doub
 //
 // dd(c) = 0.5*(q[c+1]-q[c]) + 0.5*(q[c]-q[c-1]);  d2(c) = (q[c-1]+q[c+1]) - 2*q[c]
 __device__ __forceinline__ double ppm_dd(double qm1, double q0, double qp1) {
+#if APH_EXACT
   return 0.5 * (qp1 - q0) + 0.5 * (q0 - qm1);
+#else
+  return 0.5 * (qp1 - qm1);  // the same quantity with one rounding
+#endif
 }
 __device__ __forceinline__ double ppm_d2(double qm1, double q0, double qp1) {
   return (qm1 + qp1) - 2.0 * q0;
@@ -196,8 +213,10 @@ __device__ __forceinline__ double ppm_face(double qm1, double q0, double ddm1, d
 #else
   double dph = fma(ddm1 - dd0, 1.0 / 6.0, avg);
 #endif
+#if APH_EXACT
   const double qa_tmp = dph - qm1;
   const double qb_tmp = q0 - dph;
+#endif
   const double qa = 3.0 * (qm1 + q0 - 2.0 * dph);
   double qd = 0.0;
   const bool sa = is_neg(qa);
@@ -209,13 +228,11 @@ __device__ __forceinline__ double ppm_face(double qm1, double q0, double ddm1, d
     const unsigned long long mm = mag(m), ma = mag(qa);
     qd = flip_if(from_bits(ma < mm ? ma : mm), sa);
   }
-  if (is_neg(qa_tmp * qb_tmp)) {
 #if APH_EXACT
-    dph = avg - qd / 6.0;
+  if (is_neg(qa_tmp * qb_tmp)) dph = avg - qd / 6.0;
 #else
-    dph = fma(qd, -1.0 / 6.0, avg);
+  if (strictly_outside(dph, qm1, q0)) dph = fma(qd, -1.0 / 6.0, avg);
 #endif
-  }
   return dph;
 }
 
@@ -229,9 +246,13 @@ __device__ __forceinline__ void ppm_cell(double q_im2, double q_im1, double q_i,
   double qr = dph_lo, ql = dph_hi;
   const double dqf_minus = q_i - qr;
   const double dqf_plus = ql - q_i;
+#if APH_EXACT
   const double qa_tmp = dqf_minus * dqf_plus;
   const double qb_tmp = (q_ip1 - q_i) * (q_i - q_im1);
   if (!is_pos(qa_tmp) || !is_pos(qb_tmp)) {
+#else
+  if (!strictly_between(qr, q_i, ql) || !strictly_between(q_im1, q_i, q_ip1)) {
+#endif
     // local extremum: limit with rho = qe/qd (CS eq 22-23, MC eq 27)
     double qe = 0.0;
     const bool sd = is_neg(d2qf);

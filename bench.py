@@ -58,13 +58,13 @@ WORKLOAD = ("kh3d 256^3: 64 meshblocks of 64^3, 4 ghost cells, PPM+HLLC, RK2, CF
             "gamma 5/3, FP64")
 BYTES_PER_ZONE_UPDATE = 200.0   # RK2 with 5 FP64 conserved variables
 # FP64 work of the stage kernel (fast mode) per RK2 zone-update: DADD + DMUL + DFMA thread
-# instructions from the ncu capture in profiles/stage_kernel_kh3d.md (1,160 in the stage with
-# the dt epilogue + 1,104 in the other, per zone)
-FP64_LANE_OPS_PER_ZONE_UPDATE = 2264.0
+# instructions the kernel executes, from the ncu capture in profiles/stage_kernel_kh3d.md
+# (1,020 in the stage with the dt epilogue + 961 in the other, per zone)
+FP64_LANE_OPS_PER_ZONE_UPDATE = 1981.0
 FP64_LANES_PER_CLK_PER_SM = 2.0    # DFMA lanes per clock per SM on GB300 (profiles/fp64_pipe_gb300.md)
 # DRAM bytes (read + write) per zone per stage launch, same capture (128^3 pack of 64^3 blocks;
 # the 256^3 launches process the same blocks, 8x as many)
-TRAFFIC_BYTES_PER_ZONE_LAUNCH = 613.8
+TRAFFIC_BYTES_PER_ZONE_LAUNCH = 628.3
 
 
 def peaks():
@@ -94,6 +94,9 @@ class ClockSampler:
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
                  "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
                 stderr=subprocess.DEVNULL)
+            # let nvidia-smi finish starting (its driver initialisation stalls other processes'
+            # CUDA calls for a moment) before the timed region begins
+            time.sleep(1.0)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -467,6 +470,9 @@ def main():
     ap.add_argument("--n", type=int, default=256, help="mesh cells per side")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--launch", default=None,
+                    help="JSON launch configuration of the stepper (keys of aph_stepper_config); "
+                         "used instead of the autotuner, e.g. for reproducible profiles")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-meshblock path")
     ap.add_argument("--no-amr", action="store_true", help="skip the refined-pack leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint ratio leg")
@@ -502,7 +508,12 @@ def main():
     zones = cfg.zones()
     st = Stepper(cfg, cons, exact=False)
     tune = None
-    if not args.no_tune:
+    if args.launch:
+        c = st.config
+        c.update(json.loads(args.launch))
+        st.set_config(c)
+        tune = {"config": st.config}
+    elif not args.no_tune:
         tune = st.autotune(trial_steps=1)
     stream = torch.cuda.current_stream()
     st.step(args.warmup)
@@ -551,7 +562,12 @@ def main():
         for _ in range(args.steps):
             e2e_step()
         barrier()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        t1 = time.perf_counter()  # before the sampler stops (its shutdown is not the step's)
+    e2e_ms = (t1 - t0) * 1e3 / args.steps
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
     e2e_value = zones * ws / (e2e_ms * 1e-3)
     # the host link's share of an e2e step: the load and the store alone (CUDA events)
     link = {}
@@ -624,7 +640,7 @@ def main():
                      "traffic_note": "ncu DRAM bytes per zone of a 128^3 capture x zones",
                      "kernel": "k_stage (batched stage)", "stage_ms": stage_ms,
                      "peak_source": peak_kind},
-        "fp64_pipe": {"note": "the FP64 pipe binds this kernel (ncu: 82 % busy, DRAM 2 %)",
+        "fp64_pipe": {"note": "the FP64 pipe binds this kernel (ncu: 79 % busy, DRAM 3 %); achieved counts the DADD/DMUL/DFMA it executes",
                       "peak_source": "2 DFMA lanes/clk/SM x 152 SMs x sampled SM clock"},
         "clocks": clocks,
         "time_check": {"sim_time": status["time"], "ncycle": status["ncycle"]},
