@@ -121,7 +121,7 @@ class EnsembleAdjoint(Adjoint):
         self._ens = _capi.aph_ensemble(ens.nmembers, self._member, self._gm1, None)
         self._blocks, self._table = blocks, table
         desc = _capi.aph_stepper_desc()
-        desc.params = _capi.aph_hydro_params(2, c0.ng, 5, _capi.RECON[c0.recon],
+        desc.params = _capi.aph_hydro_params(2, c0.ng, ens.nvar, _capi.RECON[c0.recon],
                                              _capi.RSOLVER[c0.rsolver], c0.gm1, c0.dfloor,
                                              c0.pfloor, c0.cfl, 0)
         desc.integrator = _capi.INTEGRATOR[c0.integrator]

@@ -53,6 +53,7 @@ class AmrConfig:
     gravity: Optional[Tuple[float, float, float]] = None
     name: str = "amr"
     ndim: int = 2
+    nscalars: int = 0   # passive scalars (hydro/composition), conserved as rho * s
 
     def __post_init__(self):
         if self.ng < RECON_NEED_GHOST[self.recon]:
@@ -69,6 +70,10 @@ class AmrConfig:
         return self.gamma - 1.0
 
     @property
+    def nvar(self):
+        return 5 + self.nscalars
+
+    @property
     def nblocks(self):
         return len(self.blocks)
 
@@ -78,11 +83,12 @@ class AmrConfig:
     def zones(self):
         return sum(B.nx[0] * B.nx[1] for B in self.blocks)
 
-    def flat_size(self, nvar=5):
-        return nvar * self.total_cells
+    def flat_size(self, nvar=None):
+        return (self.nvar if nvar is None else nvar) * self.total_cells
 
-    def block_view(self, flat, b, nvar=5):
+    def block_view(self, flat, b, nvar=None):
         """(nvar, 1, nj, ni) view of block b in a flat pack."""
+        nvar = self.nvar if nvar is None else nvar
         ni, nj = self.entire(self.blocks[b])
         o = self.offset[b] * nvar
         return flat[o:o + nvar * ni * nj].reshape(nvar, 1, nj, ni)
@@ -278,7 +284,7 @@ def _bc_array(cfg):
 
 def _params(cfg, exact):
     from . import _capi
-    return _capi.aph_hydro_params(2, cfg.ng, 5, _capi.RECON[cfg.recon], _capi.RSOLVER[cfg.rsolver],
+    return _capi.aph_hydro_params(2, cfg.ng, cfg.nvar, _capi.RECON[cfg.recon], _capi.RSOLVER[cfg.rsolver],
                                   cfg.gm1, cfg.dfloor, cfg.pfloor, cfg.cfl, 1 if exact else 0)
 
 
@@ -293,22 +299,22 @@ class AmrMeshData:
         _capi.load()
         self.cfg = cfg
         kw = dict(dtype=torch.float64, device="cuda")
-        n = cfg.total_cells
-        self.cons = torch.zeros(5 * n, **kw)
-        self.prim = torch.zeros(5 * n, **kw)
-        self.u1 = torch.zeros(5 * n, **kw)
+        n, nv = cfg.total_cells, cfg.nvar
+        self.cons = torch.zeros(nv * n, **kw)
+        self.prim = torch.zeros(nv * n, **kw)
+        self.u1 = torch.zeros(nv * n, **kw)
         self.gamma = torch.zeros(2 * n, **kw)
-        self.flux = [torch.zeros(5 * n, **kw), torch.zeros(5 * n, **kw)]
+        self.flux = [torch.zeros(nv * n, **kw), torch.zeros(nv * n, **kw)]
         blocks = (_capi.aph_block * cfg.nblocks)()
         for b, B in enumerate(cfg.blocks):
             o = cfg.offset[b]
             blk = blocks[b]
-            blk.cons = self.cons.data_ptr() + 8 * 5 * o
-            blk.prim = self.prim.data_ptr() + 8 * 5 * o
-            blk.u1 = self.u1.data_ptr() + 8 * 5 * o
+            blk.cons = self.cons.data_ptr() + 8 * nv * o
+            blk.prim = self.prim.data_ptr() + 8 * nv * o
+            blk.u1 = self.u1.data_ptr() + 8 * nv * o
             blk.gamma = self.gamma.data_ptr() + 8 * 2 * o
-            blk.flux[0] = self.flux[0].data_ptr() + 8 * 5 * o
-            blk.flux[1] = self.flux[1].data_ptr() + 8 * 5 * o
+            blk.flux[0] = self.flux[0].data_ptr() + 8 * nv * o
+            blk.flux[1] = self.flux[1].data_ptr() + 8 * nv * o
             blk.nx[:] = [B.nx[0], B.nx[1], 1]
             blk.dx[:] = [B.dx[0], B.dx[1], 1.0]
         self._blocks = blocks
@@ -426,11 +432,11 @@ class AmrStepper(_StepperBase):
         _capi.load()
         self.cfg = cfg
         self.exact = exact
-        self.cons = torch.zeros(cfg.flat_size(5), dtype=torch.float64, device="cuda")
+        self.cons = torch.zeros(cfg.flat_size(), dtype=torch.float64, device="cuda")
         self.cons.copy_(torch.as_tensor(np.ascontiguousarray(cons0)))
         blocks = (_capi.aph_block * cfg.nblocks)()
         for b, B in enumerate(cfg.blocks):
-            blocks[b].cons = self.cons.data_ptr() + 8 * 5 * cfg.offset[b]
+            blocks[b].cons = self.cons.data_ptr() + 8 * cfg.nvar * cfg.offset[b]
             blocks[b].nx[:] = [B.nx[0], B.nx[1], 1]
             blocks[b].dx[:] = [B.dx[0], B.dx[1], 1.0]
         self._blocks = blocks
@@ -451,7 +457,7 @@ class AmrStepper(_StepperBase):
         _capi.call("aph_stepper_create", ctypes.byref(desc), ctypes.byref(self.h))
 
     def interior_values(self):
-        return 5 * self.cfg.zones()
+        return self.cfg.nvar * self.cfg.zones()
 
     def tune_key(self):
         import torch
@@ -460,6 +466,26 @@ class AmrStepper(_StepperBase):
         return "%s|%s|amr|blocks%d|zones%d|levels%s|%s|%s|%s|exact%d" % (
             torch.cuda.get_device_name(), cfg.name, cfg.nblocks, cfg.zones(), levels, cfg.recon,
             cfg.rsolver, cfg.integrator, int(self.exact))
+
+
+def with_tracers(cfg, cons5, nscalars=2):
+    """(cfg, flat cons) of a refined problem with passive scalars (dyes) added: scalar k is
+    rho * s_k, s_0 a band in y and s_1 a smooth pattern in x and y (as problems.with_tracers)."""
+    import dataclasses
+    tcfg = dataclasses.replace(cfg, nscalars=nscalars)
+    cons = np.zeros(tcfg.flat_size())
+    for b in range(tcfg.nblocks):
+        src = cfg.block_view(cons5, b)
+        dst = tcfg.block_view(cons, b)
+        dst[:5] = src[:5]
+        ng = tcfg.ng
+        x, y = tcfg.cell_centers(b)
+        rho = src[0, 0, ng:-ng, ng:-ng]
+        dyes = [0.5 * (np.tanh((y - 0.25) / 0.05) - np.tanh((y - 0.75) / 0.05)),
+                0.5 + 0.25 * np.sin(2 * math.pi * x) * np.cos(2 * math.pi * y)]
+        for k in range(nscalars):
+            dst[5 + k, 0, ng:-ng, ng:-ng] = rho * dyes[k % 2]
+    return tcfg, cons
 
 
 def uniform_as_amr(cfg):
@@ -473,4 +499,4 @@ def uniform_as_amr(cfg):
     return AmrConfig(leaves, cfg.ng, tuple(cfg.mesh_nx[:2]), xmin, xmax, bc, recon=cfg.recon,
                      rsolver=cfg.rsolver, integrator=cfg.integrator, gamma=cfg.gamma, cfl=cfg.cfl,
                      dfloor=cfg.dfloor, pfloor=cfg.pfloor, gravity=cfg.gravity,
-                     name=cfg.name + "_as_amr")
+                     name=cfg.name + "_as_amr", nscalars=cfg.nscalars)

@@ -265,8 +265,7 @@ aph_status aph_pack_set_amr(aph_pack p, const aph_amr_block *amr, const int bc[6
   clear_error();
   if (!p || !amr || !bc) return fail(APH_ERR_INVALID, "NULL argument");
   if (p->parent) return fail(APH_ERR_INVALID, "set the mesh on the parent pack");
-  if (p->dev.ndim != 2 || p->dev.nvar != 5)
-    return fail(APH_ERR_UNSUPPORTED, "refined meshes are 2D with 5 variables");
+  if (p->dev.ndim != 2) return fail(APH_ERR_UNSUPPORTED, "refined meshes are 2D");
   if (p->children) return fail(APH_ERR_INVALID, "set the mesh before partitioning the pack");
   const int nb = p->dev.nblocks;
   static_assert(sizeof(AmrFaces) == sizeof(aph_amr_block), "face table layout");

@@ -60,8 +60,8 @@ __global__ void __launch_bounds__(256) k_fill_ghosts_amr(PackDev p, const BlockD
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= B.ncell) return;
   amr_fill_cell(
-      blocks, B, [](const BlockDev &X, int v, long long i) { return X.cons[v * X.ncell + i]; }, B.cons, p.bc,
-      p.ng, c);
+      blocks, B, [](const BlockDev &X, int v, long long i) { return X.cons[v * X.ncell + i]; }, B.cons,
+      p.nvar, p.bc, p.ng, c);
 }
 
 cudaError_t launch_fill_ghosts(const PackDev &p, const BlockDev *blocks, int max_ncell, int field,

@@ -58,7 +58,7 @@ struct StepBlock {
   // total energy of each cell before and after the floors of the last step's end (efl: the
   // all-ones NaN where no floor changed it), so that the next ConsToPrim floors once
   double *eraw, *efl;
-  double *bflux;      // refined meshes: fluxes of the 4 boundary faces, [face][t][5]
+  double *bflux;      // refined meshes: fluxes of the 4 boundary faces, [face][t][nvar]
   int member;         // ensembles: the member (independent problem) the block belongs to
   int nx[3];
   int ni, nj, nk;
@@ -106,7 +106,7 @@ struct StageArgs {
   int nline_items[3];
   const int *fix_items;         // refined meshes: blocks with a finer neighbour
   int nfix_items;
-  int bflux_stride;             // doubles per face of bflux (max transverse cells * 5)
+  int bflux_stride;             // doubles per face of bflux (max transverse cells * nvar)
   int cf;                       // refined meshes with coarse-fine faces: correction phases
   MemberCtl *members;           // ensembles (NULL: one problem, clock in ctl)
   const void *tmaps;            // TMA: three tensor maps (x, y, z windows) over prim, or NULL

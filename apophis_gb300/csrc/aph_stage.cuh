@@ -552,9 +552,9 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
   if (a.cf) {  // keep the boundary-face fluxes of every line for the coarse-fine correction
     const int w1 = n + 1;
     const size_t fs = (size_t)T * w1;
-    for (int it = tid; it < nl * 2 * NHYDRO; it += nth) {
-      const int t = it / (2 * NHYDRO), r = it % (2 * NHYDRO), side = r / NHYDRO, v = r % NHYDRO;
-      B.bflux[(size_t)(2 * (DIR - 1) + side) * a.bflux_stride + (size_t)(l0 + t) * NHYDRO + v] =
+    for (int it = tid; it < nl * 2 * nv; it += nth) {
+      const int t = it / (2 * nv), r = it % (2 * nv), side = r / nv, v = r % nv;
+      B.bflux[(size_t)(2 * (DIR - 1) + side) * a.bflux_stride + (size_t)(l0 + t) * nv + v] =
           F[v * fs + (size_t)t * w1 + (side == 0 ? 0 : n)];
     }
   }
@@ -663,14 +663,15 @@ __device__ void amr_correct(const StageArgs &a, const Sched &sched, unsigned int
       if (B.amr.kind[face] != FACE_FINER) continue;
       const int d = face / 2, s = face % 2, td = 1 - d;
       const double area = d == 0 ? B.dx[1] * B.dx[2] : B.dx[0] * B.dx[2];
-      for (int it2 = threadIdx.x; it2 < B.nx[td] * NHYDRO; it2 += blockDim.x) {
-        const int t = it2 / NHYDRO, v = it2 % NHYDRO;
+      const int nv = a.p.nvar;
+      for (int it2 = threadIdx.x; it2 < B.nx[td] * nv; it2 += blockDim.x) {
+        const int t = it2 / nv, v = it2 % nv;
         const int tg2 = 2 * (B.amr.origin[td] + t);
         const StepBlock &F = amr_fine_nbr(a.blocks, B, face, td, tg2);
         const int ft = tg2 - F.amr.origin[td];
         const double *fb = F.bflux + (size_t)(2 * d + 1 - s) * a.bflux_stride;
-        const double Fold = B.bflux[(size_t)face * a.bflux_stride + (size_t)t * NHYDRO + v];
-        const double Fnew = 0.5 * (fb[(size_t)ft * NHYDRO + v] + fb[(size_t)(ft + 1) * NHYDRO + v]);
+        const double Fold = B.bflux[(size_t)face * a.bflux_stride + (size_t)t * nv + v];
+        const double Fnew = 0.5 * (fb[(size_t)ft * nv + v] + fb[(size_t)(ft + 1) * nv + v]);
         const int ca = s == 0 ? 0 : B.nx[d] - 1;
         const int i = d == 0 ? ca : t, j = d == 0 ? t : ca;
         double &x = B.du[v * B.nint + (long long)j * B.nx[0] + i];
@@ -702,6 +703,13 @@ __device__ void amr_update(const StageArgs &a, const Sched &sched, unsigned int 
       const double div = -B.du[v * B.nint + ic] / vol;
       u[v] = a.gam0 * B.u0[v * nc + c] + a.gam1 * B.u1[v * nc + c] + beta_dt * div;
     }
+    bool bad = false;
+    for (int v = NHYDRO; v < p.nvar; ++v) {  // passive scalars
+      const double div = -B.du[v * B.nint + ic] / vol;
+      const double x = a.gam0 * B.u0[v * nc + c] + a.gam1 * B.u1[v * nc + c] + beta_dt * div;
+      B.u0[v * nc + c] = x;
+      bad |= ((__double_as_longlong(x) >> 52) & 0x7ff) == 0x7ff;
+    }
     if (a.gravity) {
       const double rho = B.prim[IDN * nc + c];
       u[IM1] += a.grav[0] * rho * beta_dt;
@@ -710,7 +718,6 @@ __device__ void amr_update(const StageArgs &a, const Sched &sched, unsigned int 
       de += a.grav[1] * B.prim[IV2 * nc + c];
       u[IEN] += de * rho * beta_dt;
     }
-    bool bad = false;
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v)
       bad |= ((__double_as_longlong(u[v]) >> 52) & 0x7ff) == 0x7ff;  // NaN or inf
@@ -760,7 +767,7 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
             [start](const StepBlock &X, int v, long long i) {
               return v == IEN ? energy_in(X, i, start) : X.u0[v * X.ncell + i];
             },
-            B.u0, p.bc, p.ng, c);
+            B.u0, p.nvar, p.bc, p.ng, c);
       }
       else
         ghost_cell(a, B, c);

@@ -615,8 +615,6 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   const int nvar = desc->params.nvar;
   if (amr) {
     if (ndim != 2) return fail(APH_ERR_UNSUPPORTED, "refined meshes are 2D");
-    if (nvar != 5)
-      return fail(APH_ERR_UNSUPPORTED, "packs with face tables carry no passive scalars (nvar 5)");
     std::vector<AmrFaces> faces(desc->nblocks);
     std::vector<int> nxs(2 * desc->nblocks);
     for (int b = 0; b < desc->nblocks; ++b) {
@@ -782,7 +780,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
       e = cudaMemcpy(s->d_members, members.data(), sizeof(MemberCtl) * members.size(), cudaMemcpyHostToDevice);
   }
   if (amr) {
-    s->bflux_stride = 5 * std::max(p.max_nx[0], p.max_nx[1]);
+    s->bflux_stride = nvar * std::max(p.max_nx[0], p.max_nx[1]);
     ck(cudaMalloc(&s->d_bflux, sizeof(double) * 4 * s->bflux_stride * p.nblocks));
     std::vector<int> fix;
     for (int b = 0; b < p.nblocks; ++b)

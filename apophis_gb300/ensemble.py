@@ -49,7 +49,7 @@ class Ensemble:
         self.total_cells = off
         first = self.members[0]
         for cfg in self.members:
-            for attr in ("ng", "recon", "rsolver", "integrator", "cfl", "dfloor", "pfloor"):
+            for attr in ("ng", "recon", "rsolver", "integrator", "cfl", "dfloor", "pfloor", "nscalars"):
                 if getattr(cfg, attr) != getattr(first, attr):
                     raise ValueError("ensemble members share %s" % attr)
 
@@ -57,23 +57,27 @@ class Ensemble:
     def nmembers(self):
         return len(self.members)
 
+    @property
+    def nvar(self):
+        return self.members[0].nvar
+
     def zones(self):
         return sum(c.zones() for c in self.members)
 
     def member_slice(self, m):
-        """Slice of the flat pack (5 values per cell) holding member m."""
-        start = 5 * self.offset[self.block0[m]]
-        return slice(start, start + 5 * self.mesh[m].total_cells)
+        """Slice of the flat pack (nvar values per cell) holding member m."""
+        start = self.nvar * self.offset[self.block0[m]]
+        return slice(start, start + self.nvar * self.mesh[m].total_cells)
 
     def pack(self, conses):
-        """Flat pack from the members' (nblocks, 5, nk, nj, ni) arrays."""
-        out = np.empty(5 * self.total_cells)
+        """Flat pack from the members' (nblocks, nvar, nk, nj, ni) arrays."""
+        out = np.empty(self.nvar * self.total_cells)
         for m, c in enumerate(conses):
             out[self.member_slice(m)] = np.ascontiguousarray(c).reshape(-1)
         return out
 
     def unpack(self, flat, m):
-        return flat[self.member_slice(m)].reshape(self.members[m].pack_shape(5))
+        return flat[self.member_slice(m)].reshape(self.members[m].pack_shape(self.nvar))
 
     def blocks(self):
         """(AmrBlock with pack-wide neighbour indices, member) per block."""
@@ -110,7 +114,7 @@ class EnsembleStepper(_StepperBase):
     member with its own gas constants, dt and clock (finished members are skipped)."""
 
     def interior_values(self):
-        return 5 * sum(c.zones() for c in self.ens.members)
+        return self.ens.nvar * sum(c.zones() for c in self.ens.members)
 
     def __init__(self, ens: Ensemble, cons0, exact=False, fixed_dt=0.0):
         import torch
@@ -121,13 +125,14 @@ class EnsembleStepper(_StepperBase):
         self.ens = ens
         self.cfg = ens.members[0]
         self.exact = exact
-        self.cons = torch.zeros(5 * ens.total_cells, dtype=torch.float64, device="cuda")
+        nv = ens.nvar
+        self.cons = torch.zeros(nv * ens.total_cells, dtype=torch.float64, device="cuda")
         self.cons.copy_(torch.as_tensor(np.ascontiguousarray(cons0)))
         nb = ens.nblocks
         blks = ens.blocks()
         blocks = (_capi.aph_block * nb)()
         for b, B in enumerate(blks):
-            blocks[b].cons = self.cons.data_ptr() + 8 * 5 * ens.offset[b]
+            blocks[b].cons = self.cons.data_ptr() + 8 * nv * ens.offset[b]
             blocks[b].nx[:] = [B.nx[0], B.nx[1], 1]
             blocks[b].dx[:] = [B.dx[0], B.dx[1], 1.0]
         table = self.face_table(blks)
@@ -138,7 +143,7 @@ class EnsembleStepper(_StepperBase):
         self._blocks, self._table = blocks, table
         c0 = ens.members[0]
         desc = _capi.aph_stepper_desc()
-        desc.params = _capi.aph_hydro_params(2, c0.ng, 5, _capi.RECON[c0.recon],
+        desc.params = _capi.aph_hydro_params(2, c0.ng, nv, _capi.RECON[c0.recon],
                                              _capi.RSOLVER[c0.rsolver], c0.gm1, c0.dfloor,
                                              c0.pfloor, c0.cfl, 1 if exact else 0)
         desc.integrator = _capi.INTEGRATOR[c0.integrator]

@@ -703,6 +703,7 @@ struct AmrBlock {
 };
 
 struct AmrMesh {
+  int nvar = 5;  // 5 hydro variables, then the passive scalars
   int ng, recon, rsolver, integrator, bc[2][2], gravity;
   Real gm1, cfl, dfloor, pfloor, g[3];
   std::vector<AmrBlock> blocks;
@@ -722,14 +723,14 @@ static inline size_t ACELL(const AmrBlock &B, int d, int a, int t) {
 }
 static inline Real AU(const AmrMesh &m, const std::vector<Real> &q, const AmrBlock &B, int v,
                       size_t cell) {
-  return q[B.off * 5 + (size_t)v * B.d.ncell + cell];
+  return q[B.off * m.nvar + (size_t)v * B.d.ncell + cell];
 }
 static inline Real minmod(Real a, Real b) {
   if (!(a * b > 0.0)) return 0.0;
   return (std::abs(a) < std::abs(b)) ? a : b;
 }
 
-// Ghost value of all 5 components for face (d, s) of block B at depth k, transverse index t.
+// Ghost value of all nvar components for face (d, s) of block B at depth k, transverse index t.
 static void amr_ghost(const AmrMesh &m, const std::vector<Real> &q, const AmrBlock &B, int d,
                       int s, int k, int t, Real *out) {
   const int face = 2 * d + s, td = 1 - d;
@@ -738,15 +739,15 @@ static void amr_ghost(const AmrMesh &m, const std::vector<Real> &q, const AmrBlo
     const AmrBlock &N = m.blocks[B.nbr[face][0]];
     const int a = s == 0 ? N.nx[d] - 1 - k : k;
     const int tn = B.origin[td] + t - N.origin[td];
-    for (int v = 0; v < 5; ++v) out[v] = AU(m, q, N, v, ACELL(N, d, a, tn));
+    for (int v = 0; v < m.nvar; ++v) out[v] = AU(m, q, N, v, ACELL(N, d, a, tn));
   } else if (kind == FACE_BOUNDARY) {
     const int bcv = m.bc[d][s];
     if (bcv == BC_OUTFLOW) {
       const int a = s == 0 ? 0 : B.nx[d] - 1;
-      for (int v = 0; v < 5; ++v) out[v] = AU(m, q, B, v, ACELL(B, d, a, t));
+      for (int v = 0; v < m.nvar; ++v) out[v] = AU(m, q, B, v, ACELL(B, d, a, t));
     } else {
       const int a = s == 0 ? k : B.nx[d] - 1 - k;
-      for (int v = 0; v < 5; ++v) {
+      for (int v = 0; v < m.nvar; ++v) {
         const Real x = AU(m, q, B, v, ACELL(B, d, a, t));
         out[v] = (v == 1 + d) ? -x : x;
       }
@@ -761,7 +762,7 @@ static void amr_ghost(const AmrMesh &m, const std::vector<Real> &q, const AmrBlo
     const int ft = tg2 - F->origin[td];
     const int a0 = s == 0 ? F->nx[d] - 1 - 2 * k : 2 * k;
     const int a1 = s == 0 ? a0 - 1 : a0 + 1;
-    for (int v = 0; v < 5; ++v)
+    for (int v = 0; v < m.nvar; ++v)
       out[v] = ((AU(m, q, *F, v, ACELL(*F, d, a0, ft)) + AU(m, q, *F, v, ACELL(*F, d, a0, ft + 1))) +
                 (AU(m, q, *F, v, ACELL(*F, d, a1, ft)) + AU(m, q, *F, v, ACELL(*F, d, a1, ft + 1)))) *
                0.25;
@@ -775,7 +776,7 @@ static void amr_ghost(const AmrMesh &m, const std::vector<Real> &q, const AmrBlo
     const int gf = s == 0 ? B.origin[d] - 1 - k : B.origin[d] + B.nx[d] + k;
     const Real on = (gf & 1) ? 0.25 : -0.25;
     const Real ot = (tg & 1) ? 0.25 : -0.25;
-    for (int v = 0; v < 5; ++v) {
+    for (int v = 0; v < m.nvar; ++v) {
       const Real c = AU(m, q, C, v, ACELL(C, d, ic, tc));
       // neighbours along +d / -d in the coarse block's index space
       Real cm, cp;
@@ -808,7 +809,7 @@ static void amr_fill_ghosts(AmrMesh &m, std::vector<Real> &q) {
   for (int b = 0; b < (int)m.blocks.size(); ++b) {
     const AmrBlock &B = m.blocks[b];
     const Dims &d = B.d;
-    Real val[5];
+    Real val[64];
     for (int j = 0; j < d.nj; ++j)
       for (int i = 0; i < d.ni; ++i) {
         const bool gi = i < d.ng || i >= d.ng + B.nx[0];
@@ -818,7 +819,7 @@ static void amr_fill_ghosts(AmrMesh &m, std::vector<Real> &q) {
         if (gi && gj) {
           const int ci = std::min(std::max(i, d.ng), d.ng + B.nx[0] - 1);
           const int cj = std::min(std::max(j, d.ng), d.ng + B.nx[1] - 1);
-          for (int v = 0; v < 5; ++v) val[v] = AU(m, q, B, v, (size_t)cj * d.ni + ci);
+          for (int v = 0; v < m.nvar; ++v) val[v] = AU(m, q, B, v, (size_t)cj * d.ni + ci);
         } else if (gi) {
           const int s = i < d.ng ? 0 : 1;
           const int k = s == 0 ? d.ng - 1 - i : i - (d.ng + B.nx[0]);
@@ -828,20 +829,20 @@ static void amr_fill_ghosts(AmrMesh &m, std::vector<Real> &q) {
           const int k = s == 0 ? d.ng - 1 - j : j - (d.ng + B.nx[1]);
           amr_ghost(m, q, B, 1, s, k, i - d.ng, val);
         }
-        for (int v = 0; v < 5; ++v) q[B.off * 5 + (size_t)v * d.ncell + cell] = val[v];
+        for (int v = 0; v < m.nvar; ++v) q[B.off * m.nvar + (size_t)v * d.ncell + cell] = val[v];
       }
   }
 }
 
 static void amr_fill_derived(AmrMesh &m) {
   for (const AmrBlock &B : m.blocks)
-    cons_to_prim(B.d, &m.u0[B.off * 5], &m.prim[B.off * 5], &m.gamma[B.off * 2], m.gm1, m.dfloor, m.pfloor);
+    cons_to_prim(B.d, &m.u0[B.off * m.nvar], &m.prim[B.off * m.nvar], &m.gamma[B.off * 2], m.gm1, m.dfloor, m.pfloor);
 }
 
 static Real amr_estimate_dt(AmrMesh &m) {
   Real mn = std::numeric_limits<Real>::max();
   for (AmrBlock &B : m.blocks)
-    mn = std::min(mn, m.cfl * estimate_timestep_min(B.d, &m.prim[B.off * 5], &m.u0[B.off * 5], B.dx, m.gm1));
+    mn = std::min(mn, m.cfl * estimate_timestep_min(B.d, &m.prim[B.off * m.nvar], &m.u0[B.off * m.nvar], B.dx, m.gm1));
   return mn;
 }
 
@@ -855,8 +856,8 @@ static void amr_step(AmrMesh &m, Real dt) {
     const int nb = (int)m.blocks.size();
     for (int b = 0; b < nb; ++b) {
       AmrBlock &B = m.blocks[b];
-      calculate_fluxes(B.d, recon, m.rsolver, &m.prim[B.off * 5], &m.gamma[B.off * 2],
-                       &m.flux[0][B.off * 5], &m.flux[1][B.off * 5], nullptr);
+      calculate_fluxes(B.d, recon, m.rsolver, &m.prim[B.off * m.nvar], &m.gamma[B.off * 2],
+                       &m.flux[0][B.off * m.nvar], &m.flux[1][B.off * m.nvar], nullptr);
     }
     // flux differences, x then y
 #pragma omp parallel for schedule(dynamic, 4)
@@ -864,10 +865,10 @@ static void amr_step(AmrMesh &m, Real dt) {
       AmrBlock &B = m.blocks[b];
       const Dims &d = B.d;
       const Real a1 = B.dx[1] * B.dx[2], a2 = B.dx[0] * B.dx[2];
-      const Real *F1 = &m.flux[0][B.off * 5], *F2 = &m.flux[1][B.off * 5];
+      const Real *F1 = &m.flux[0][B.off * m.nvar], *F2 = &m.flux[1][B.off * m.nvar];
       Real *du = &m.du[m.du_off[b]];
       const size_t nint = (size_t)B.nx[0] * B.nx[1];
-      for (int v = 0; v < 5; ++v)
+      for (int v = 0; v < m.nvar; ++v)
         for (int j = 0; j < B.nx[1]; ++j)
           for (int i = 0; i < B.nx[0]; ++i) {
             const size_t c = IX(d, v, 0, j + d.ng, i + d.ng);
@@ -886,7 +887,7 @@ static void amr_step(AmrMesh &m, Real dt) {
         if (B.kind[face] != FACE_FINER || m.plant_no_correction) continue;
         const int d = face / 2, s = face % 2, td = 1 - d;
         const Real area = d == 0 ? B.dx[1] * B.dx[2] : B.dx[0] * B.dx[2];
-        const Real *Fb = &m.flux[d][B.off * 5];
+        const Real *Fb = &m.flux[d][B.off * m.nvar];
         for (int t = 0; t < B.nx[td]; ++t) {
           const int tg2 = 2 * (B.origin[td] + t);
           const AmrBlock *F = nullptr;
@@ -895,12 +896,12 @@ static void amr_step(AmrMesh &m, Real dt) {
             if (tg2 >= C.origin[td] && tg2 < C.origin[td] + C.nx[td]) F = &C;
           }
           const int ft = tg2 - F->origin[td];
-          const Real *Ff = &m.flux[d][F->off * 5];
+          const Real *Ff = &m.flux[d][F->off * m.nvar];
           // face index (along d) of the shared face in each block
           const int fb = s == 0 ? 0 : B.nx[d];
           const int ff = s == 0 ? F->nx[d] : 0;
           const int a = s == 0 ? 0 : B.nx[d] - 1;  // coarse boundary cell
-          for (int v = 0; v < 5; ++v) {
+          for (int v = 0; v < m.nvar; ++v) {
             auto fidx = [&](const AmrBlock &X, int fa, int tt) {
               const int i = d == 0 ? X.d.ng + fa : X.d.ng + tt;
               const int j = d == 0 ? X.d.ng + tt : X.d.ng + fa;
@@ -923,16 +924,16 @@ static void amr_step(AmrMesh &m, Real dt) {
       const Real vol = B.dx[0] * B.dx[1] * B.dx[2];
       const Real *du = &m.du[m.du_off[b]];
       const size_t nint = (size_t)B.nx[0] * B.nx[1];
-      Real *u0 = &m.u0[B.off * 5];
-      const Real *u1 = &m.u1[B.off * 5];
-      for (int v = 0; v < 5; ++v)
+      Real *u0 = &m.u0[B.off * m.nvar];
+      const Real *u1 = &m.u1[B.off * m.nvar];
+      for (int v = 0; v < m.nvar; ++v)
         for (int j = 0; j < B.nx[1]; ++j)
           for (int i = 0; i < B.nx[0]; ++i) {
             const size_t c = IX(d, v, 0, j + d.ng, i + d.ng);
             const Real div = -du[v * nint + (size_t)j * B.nx[0] + i] / vol;
             u0[c] = gam0 * u0[c] + gam1 * u1[c] + beta * dt * div;
           }
-      if (m.gravity) apply_gravity(d, u0, &m.prim[B.off * 5], m.g, beta * dt);
+      if (m.gravity) apply_gravity(d, u0, &m.prim[B.off * m.nvar], m.g, beta * dt);
     }
     amr_fill_ghosts(m, m.u0);
     amr_fill_derived(m);
@@ -1057,7 +1058,7 @@ void orc_mesh_state(void *h, double *out3) {
 
 
 // ---- refined mesh driver ------------------------------------------------------------------
-// ints: [nblocks, ng, recon, rsolver, integrator, bc x1i, x1o, x2i, x2o, gravity]
+// ints: [nblocks, ng, recon, rsolver, integrator, bc x1i, x1o, x2i, x2o, gravity, nvar]
 // blk (per block 1+2+2+4+4+16 = 29 ints): level, origin[2], nx[2], kind[4], cnt[4], nbr[4][4]
 // reals: [gm1, cfl, dfloor, pfloor, g1, g2, g3]; bdx: per block dx1, dx2, dx3
 void *orc_amr_create(const int *ints, const int *blk, const double *reals, const double *bdx) {
@@ -1066,6 +1067,8 @@ void *orc_amr_create(const int *ints, const int *blk, const double *reals, const
   m->ng = ints[1]; m->recon = ints[2]; m->rsolver = ints[3]; m->integrator = ints[4];
   m->bc[0][0] = ints[5]; m->bc[0][1] = ints[6]; m->bc[1][0] = ints[7]; m->bc[1][1] = ints[8];
   m->gravity = ints[9];
+  m->nvar = ints[10];
+  const int nv = m->nvar;
   m->gm1 = reals[0]; m->cfl = reals[1]; m->dfloor = reals[2]; m->pfloor = reals[3];
   for (int d = 0; d < 3; ++d) m->g[d] = reals[4 + d];
   m->blocks.resize(nb);
@@ -1077,15 +1080,15 @@ void *orc_amr_create(const int *ints, const int *blk, const double *reals, const
     for (int f = 0; f < 4; ++f) { B.kind[f] = p[5 + f]; B.cnt[f] = p[9 + f]; }
     for (int f = 0; f < 4; ++f) for (int n = 0; n < 4; ++n) B.nbr[f][n] = p[13 + 4 * f + n];
     for (int d = 0; d < 3; ++d) B.dx[d] = bdx[3 * b + d];
-    B.d = make_dims(5, B.nx[0], B.nx[1], 1, m->ng, 2);
+    B.d = make_dims(nv, B.nx[0], B.nx[1], 1, m->ng, 2);
     B.off = off;
     off += B.d.ncell;
     m->du_off.push_back(doff);
-    doff += (size_t)5 * B.nx[0] * B.nx[1];
+    doff += (size_t)nv * B.nx[0] * B.nx[1];
   }
   m->total = off;
-  m->u0.assign(5 * off, 0.0); m->u1.assign(5 * off, 0.0); m->prim.assign(5 * off, 0.0);
-  m->gamma.assign(2 * off, 0.0); m->flux[0].assign(5 * off, 0.0); m->flux[1].assign(5 * off, 0.0);
+  m->u0.assign(nv * off, 0.0); m->u1.assign(nv * off, 0.0); m->prim.assign(nv * off, 0.0);
+  m->gamma.assign(2 * off, 0.0); m->flux[0].assign(nv * off, 0.0); m->flux[1].assign(nv * off, 0.0);
   m->du.assign(doff, 0.0);
   return m;
 }

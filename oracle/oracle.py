@@ -169,7 +169,7 @@ class AmrMesh:
         bc = cfg.bc
         ints = [cfg.nblocks, cfg.ng, RECON[cfg.recon], RSOLVER[cfg.rsolver],
                 INTEGRATOR[cfg.integrator], BC[bc[0][0]], BC[bc[0][1]], BC[bc[1][0]],
-                BC[bc[1][1]], 1 if cfg.gravity is not None else 0]
+                BC[bc[1][1]], 1 if cfg.gravity is not None else 0, cfg.nvar]
         blk = []
         bdx = []
         for B in cfg.blocks:
@@ -201,11 +201,11 @@ class AmrMesh:
 
     def set_cons(self, cons):
         c = np.ascontiguousarray(cons, dtype=np.float64)
-        assert c.size == self.cfg.flat_size(5)
+        assert c.size == self.cfg.flat_size()
         lib().orc_amr_set_cons(self.h, _p(c))
 
     def get(self, what="cons"):
-        out = np.empty(self.cfg.flat_size(5))
+        out = np.empty(self.cfg.flat_size())
         lib().orc_amr_get(self.h, 0 if what == "cons" else 1, _p(out))
         return out
 

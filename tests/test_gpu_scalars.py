@@ -107,3 +107,80 @@ def test_scalars_rejected_where_not_carried(cuda):
     cfg, cons = problems.kh2d_tracers(n=32, block=16, ng=2)
     with pytest.raises(Exception, match="passive scalars"):
         adjoint.Adjoint(cfg)
+
+
+def _amr_interiors(cfg, flat):
+    ng = cfg.ng
+    return np.concatenate([cfg.block_view(flat, b)[:, 0, ng:-ng, ng:-ng].reshape(cfg.nvar, -1)
+                           for b in range(cfg.nblocks)], axis=1)
+
+
+@pytest.mark.parametrize("path", ["pack", "block", "stepper"])
+def test_scalars_refined_mesh_exact(cuda, path):
+    """Passive scalars on the two-level mesh: ghost map (copy, restriction, prolongation) and
+    coarse-fine flux correction of the scalars, bit-identical to the refined-mesh oracle."""
+    from apophis_gb300 import amr
+    cfg, cons = amr.with_tracers(*amr.small_test_mesh(), nscalars=2)
+    m = O.AmrMesh(cfg)
+    m.set_cons(cons)
+    m.run(nsteps=4)
+    if path == "stepper":
+        s = amr.AmrStepper(cfg, cons, exact=True)
+        s.step(4)
+        assert s.status()["time"] == m.state()["time"]
+        got = s.state()
+        s.close()
+    else:
+        d = amr.AmrDriver(cfg, cons, exact=True, per_block=(path == "block"))
+        d.run(nsteps=4)
+        assert d.time == m.state()["time"]
+        got = d.cons()
+        d.md.close()
+    assert np.array_equal(_amr_interiors(cfg, got), _amr_interiors(cfg, m.get()))
+
+
+def test_scalars_refined_mesh_fast_and_conserved(cuda):
+    from apophis_gb300 import amr
+    cfg, cons = amr.with_tracers(*amr.small_test_mesh(), nscalars=2)
+    m = O.AmrMesh(cfg)
+    m.set_cons(cons)
+    m.run(nsteps=1)
+    s = amr.AmrStepper(cfg, cons, exact=False)
+    s.step(1)
+    g, w = _amr_interiors(cfg, s.state()), _amr_interiors(cfg, m.get())
+    for v in range(cfg.nvar):
+        scale = np.abs(w[1:4]).max() if 1 <= v <= 3 else np.abs(w[v]).max()
+        assert np.abs(g[v] - w[v]).max() <= 1e-12 * scale, v
+    vol = np.concatenate([np.full(B.nx[0] * B.nx[1], B.dx[0] * B.dx[1]) for B in cfg.blocks])
+    before = (_amr_interiors(cfg, cons)[5:] * vol).sum(axis=1)
+    s.step(20)
+    after = (_amr_interiors(cfg, s.state())[5:] * vol).sum(axis=1)
+    assert np.all(np.abs(after - before) <= 1e-12 * np.abs(before))
+    s.close()
+
+
+def test_scalars_ensemble_members_match_oracle(cuda):
+    """An ensemble whose members carry passive scalars: every member bit-identical (exact) to
+    the oracle run of that member alone."""
+    from apophis_gb300 import ensemble
+    rng = np.random.Generator(np.random.PCG64(5))
+    cfgs, conses = [], []
+    for n in (32, 48, 32):
+        cfg, cons = problems.with_tracers(*problems.blast2d(
+            n=n, block=16, ng=4, r0=float(rng.uniform(0.1, 0.3)),
+            gamma=float(rng.uniform(1.4, 5.0 / 3.0))), nscalars=2)
+        cfgs.append(cfg)
+        conses.append(cons)
+    ens = ensemble.Ensemble(cfgs, [0.05] * len(cfgs))
+    st = ensemble.EnsembleStepper(ens, ens.pack(conses), exact=True)
+    st.step(4)
+    got = st.state()
+    for m, cfg in enumerate(cfgs):
+        o = O.Mesh(cfg)
+        o.set_cons(conses[m])
+        o.run(nsteps=4)
+        assert np.array_equal(_interior(cfg, ens.unpack(got, m)), _interior(cfg, o.get())), m
+    st.close()
+    from apophis_gb300 import adjoint
+    with pytest.raises(Exception, match="passive scalars"):
+        adjoint.EnsembleAdjoint(ens)
