@@ -131,3 +131,31 @@ def _mass(cfg, flat):
     ng = cfg.ng
     return sum(cfg.block_view(flat, b)[0, 0, ng:-ng, ng:-ng].sum() * B.dx[0] * B.dx[1]
                for b, B in enumerate(cfg.blocks))
+
+
+def test_refined_stepper_interiors_round_trip(cuda):
+    """Packed interiors of uneven blocks (16^2 and 32^2): out, back in, and stepping on."""
+    import torch
+    cfg, cons = amr.rt2d_amr(nx=64, ny=192, block0=32, blockf=16)
+    a = amr.AmrStepper(cfg, cons, exact=True)
+    b = amr.AmrStepper(cfg, cons, exact=True)
+    buf = torch.empty(b.interior_values(), dtype=torch.float64, pin_memory=True)
+    for _ in range(3):
+        a.step(1)
+        b.step(1)
+        b.store_interiors(buf)
+        b.load_interiors(buf)
+    torch.cuda.synchronize()
+    packed = buf.numpy()
+    # the packed layout: block after block, each (nvar, ny, nx) interior cells
+    off, ng = 0, cfg.ng
+    for blk in range(cfg.nblocks):
+        B = cfg.blocks[blk]
+        n = 5 * B.nx[0] * B.nx[1]
+        want = cfg.block_view(a.state(), blk)[:, 0, ng:-ng, ng:-ng].reshape(-1)
+        assert np.array_equal(packed[off:off + n], want), blk
+        off += n
+    assert off == packed.size
+    assert np.array_equal(_interiors(cfg, a.state()), _interiors(cfg, b.state()))
+    a.close()
+    b.close()
