@@ -1172,7 +1172,7 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
       for (const StepBlock &B : s->hblocks)
         most = std::max(most, d == 0 ? B.nx[1] * B.nx[2] : d == 1 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1]);
     most = std::min(most, 64);
-    int prev_occ = 0, prev_T = 0;
+    int prev_occ = 0, prev_T = 0, T_low_edge = 0;
     for (int T = tma ? 2 : 1; T <= most + 1; T += tma ? 2 : 1) {
       int occ = 0;
       if (T <= most) {
@@ -1183,13 +1183,19 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
           occ = stage_residency(s, threads, reg_cap, smem);
       }
       if (occ != prev_occ && prev_occ > 0 && prev_occ * threads >= 256) {
-        aph_stepper_config c = from;
-        c.threads = threads;
-        c.reg_cap = reg_cap;
-        c.tma = tma;
-        c.ctas_per_sm = 0;
-        for (int d = 0; d < 3; ++d) c.lines[d] = d < ndim ? prev_T : 0;
-        out.push_back(c);
+        // the edge, and the count below it (a pass item's loops end in a partly filled round
+        // of warps, which a smaller count at the same residency may fill better)
+        for (int Tc : {prev_T, prev_T - (tma ? 2 : 1)}) {
+          if (Tc < 1 || (Tc != prev_T && Tc == T_low_edge)) continue;
+          aph_stepper_config c = from;
+          c.threads = threads;
+          c.reg_cap = reg_cap;
+          c.tma = tma;
+          c.ctas_per_sm = 0;
+          for (int d = 0; d < 3; ++d) c.lines[d] = d < ndim ? Tc : 0;
+          out.push_back(c);
+        }
+        T_low_edge = prev_T;
       }
       if (occ == 0 && prev_occ > 0) break;
       prev_occ = occ;
