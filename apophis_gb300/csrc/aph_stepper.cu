@@ -1203,7 +1203,7 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
     }
     return out;
   };
-  // round 1: launch shapes with plain loads, strided schedule, x-y-z order
+  // first candidate set: launch shapes with plain loads, strided schedule, x-y-z order
   {
     aph_stepper_config c0 = base;
     c0.schedule = 0;
@@ -1219,7 +1219,7 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
     if (cands.empty()) cands.push_back(c0);
     trial(cands);
   }
-  // round 2: schedules and sweep orders (any order only in fast mode: exact mode keeps the
+  // second set: schedules and sweep orders (any order only in fast mode: exact mode keeps the
   // reference's x, y, z summation) around the best shape
   {
     std::vector<std::vector<int>> orders = {{1, 2, 3}};
@@ -1239,7 +1239,7 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
       }
     trial(cands);
   }
-  // round 3: TMA-staged windows (even line counts) with the best schedule and order; fast
+  // third set: TMA-staged windows (even line counts) with the best schedule and order; fast
   // mode only (exact mode reconstructs the gamma field, which the windows do not carry)
   if (!s->params.exact) {
     const aph_stepper_config b = best_c;

@@ -62,7 +62,7 @@ def test_stepper_integrators_exact(cuda, integ):
 
 
 def test_stepper_sod_to_tlim(cuda):
-    """configs[0]: Sod 1D to t = 0.2 in the batched path, L1(rho) vs oracle < 1e-10."""
+    """Sod 1D (256 cells, PLM+HLLE) to t = 0.2 in the batched path, L1(rho) vs oracle < 1e-10."""
     cfg, cons = problems.sod(nx=256, recon="plm", rsolver="hlle", integrator="rk2", cfl=0.4)
     m = O.Mesh(cfg)
     m.set_cons(cons)
