@@ -72,7 +72,8 @@ class HaloPlan:
     recv_sign: Dict[int, np.ndarray]
 
 
-def plan_halo(cfg: MeshConfig, parts: List[List[int]], rank: int, nvar: int = 5) -> HaloPlan:
+def plan_halo(cfg: MeshConfig, parts: List[List[int]], rank: int, nvar: int = None) -> HaloPlan:
+    nvar = cfg.nvar if nvar is None else nvar  # 5 hydro variables, then the passive scalars
     ng, nd = cfg.ng, cfg.ndim
     bn = cfg.block_nx
     nb = cfg.blocks_per_dim

@@ -26,6 +26,8 @@ def _case(name):
         return problems.kh2d(n=32, block=8, ng=2)
     if name == "rt2d":
         return problems.rt2d(nx=16, ny=48, block=(8, 8), ng=3)
+    if name == "kh2d_tracers":  # passive scalars ride along in the exchange
+        return problems.kh2d_tracers(n=32, block=8, ng=2)
     cfg = MeshConfig(ndim=3, mesh_nx=(16, 16, 16), block_nx=(8, 8, 8), ng=2,
                      bc=(("periodic", "periodic"), ("outflow", "reflecting"), ("reflecting", "outflow")),
                      recon="plm", rsolver="hlle")
@@ -62,7 +64,7 @@ def _worker(rank, world, port, name, q):
         dist.destroy_process_group()
 
 
-@pytest.mark.parametrize("name", ["kh2d", "rt2d", "box3d"])
+@pytest.mark.parametrize("name", ["kh2d", "rt2d", "box3d", "kh2d_tracers"])
 def test_two_rank_exchange_matches_oracle(name):
     from oracle import oracle as O
     cfg, cons = _case(name)
