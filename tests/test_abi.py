@@ -93,6 +93,21 @@ def test_null_pack_calls_fail_cleanly():
     assert lib.aph_pack_destroy(None) == 0
 
 
+def test_null_stepper_calls_fail_cleanly():
+    """Every stepper entry point checks its handle before any device work."""
+    lib = _capi.load()
+    d = ctypes.c_double()
+    buf = (ctypes.c_double * 8)()
+    assert lib.aph_stepper_step(None, 1, None) == 1
+    assert lib.aph_stepper_status(None, ctypes.byref(d), ctypes.byref(d), None, None) == 1
+    assert lib.aph_stepper_history(None, buf, None) == 1
+    assert lib.aph_stepper_load_interiors(None, buf, None) == 1
+    assert lib.aph_stepper_store_interiors(None, buf, None) == 1
+    assert lib.aph_stepper_set_clock(None, 0.0, 0.0, 0, None) == 1
+    assert lib.aph_stepper_destroy(None) == 0
+    assert "NULL" in lib.aph_last_error().decode()
+
+
 def test_stepper_rejects_bad_ensembles():
     """Validation runs before any device work, so it is checked without a GPU."""
     import ctypes
