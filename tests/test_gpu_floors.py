@@ -84,3 +84,25 @@ def test_floors_fast_bit_identical_across_line_counts(cuda):
             st.close()
     for out, status in outs[1:]:
         assert np.array_equal(out, outs[0][0]) and status == outs[0][1]
+
+
+def test_floors_with_face_tables_exact(cuda):
+    """Floors firing on a pack described by face tables (the refined-mesh ghost map, here on an
+    unrefined mesh): the batched stepper stays bit-identical to the refined-mesh oracle, which
+    equals the uniform one."""
+    from apophis_gb300 import amr
+    cfg, cons = problems.rarefaction2d()
+    acfg = amr.uniform_as_amr(cfg)
+    flat = np.ascontiguousarray(cons).reshape(-1)
+    m = O.AmrMesh(acfg)
+    m.set_cons(flat)
+    st = amr.AmrStepper(acfg, flat, exact=True)
+    ng = acfg.ng
+    for _ in range(6):
+        m.run(nsteps=1)
+        st.step(1)
+        got, want = st.state(), m.get()
+        for b in range(acfg.nblocks):
+            assert np.array_equal(acfg.block_view(got, b)[:, 0, ng:-ng, ng:-ng],
+                                  acfg.block_view(want, b)[:, 0, ng:-ng, ng:-ng]), b
+    st.close()
