@@ -354,7 +354,7 @@ __device__ void hlle_vjp(const double *wl, const double *wr, const GasConsts &gc
   gwr[IPR] += gcr * sr.dc_dp; gwr[IDN] += gcr * sr.dc_drho;
 }
 
-// ---- HLLC (hydro_hllc.hpp:161-282) -----------------------------------------------------------
+// ---- HLLC (hydro_hllc.hpp:14-146) -----------------------------------------------------------
 __device__ void hllc_vjp(const double *wl, const double *wr, const GasConsts &gc, double ic2g,
                          const double *gf, double *gwl, double *gwr) {
   const double igm1 = gc.igm1;

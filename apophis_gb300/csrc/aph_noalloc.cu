@@ -2,11 +2,13 @@
 //
 // Some callers cannot allocate device memory at the moment they need a timestep: a host
 // code that hands all of its device memory to its own pool allocator up front (a Kokkos
-// or Parthenon application sized to the GPU), or a step that is being recorded into a CUDA
-// graph, where cudaMalloc is not a capturable operation and synchronises the device.  This
+// or Parthenon application sized to the GPU) has none left for cudaMalloc, and a call of
+// cudaMalloc or cudaFree in the middle of its step would also synchronise the device.  This
 // entry point keeps its scratch -- one partial minimum per CTA -- in a file-scope device
 // array, so that neither it nor anything it calls allocates.  The array lives as long as
 // the library is loaded, on every GPU that loads it.
+#include <cuda.h>
+
 #include <cfloat>
 #include <mutex>
 
@@ -25,24 +27,58 @@ constexpr int kMaxDevices = 64;
 // Shared by every call on a device; each call overwrites the first nctas entries.
 static __device__ __align__(256) unsigned long long g_dt_partials[kMaxCtas];
 
+// The driver's context queries, taken through the runtime (no link against libcuda).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
 struct DeviceScratch {
   std::mutex mu;
+  CtxGetCurrentFn ctx_current = nullptr;
+  CtxGetIdFn ctx_id = nullptr;
+  bool looked_up = false;
   unsigned long long *ptr[kMaxDevices] = {};
+  unsigned long long ctx[kMaxDevices] = {};  // the context the address belongs to
 };
 DeviceScratch g_scratch;
 
-// Device address of g_dt_partials on the current device (set up on the first call there).
+// Identity of the calling thread's current context (0 if none or unknown).
+unsigned long long current_context_id() {
+  if (!g_scratch.looked_up) {
+    g_scratch.looked_up = true;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      g_scratch.ctx_current = (CtxGetCurrentFn)fn;
+    fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      g_scratch.ctx_id = (CtxGetIdFn)fn;
+  }
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!g_scratch.ctx_current || !g_scratch.ctx_id || g_scratch.ctx_current(&c) != CUDA_SUCCESS || !c)
+    return 0;
+  if (g_scratch.ctx_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of g_dt_partials on the current device.  It is looked up on the first call
+// there, and again whenever the device's context is no longer the one it was looked up in
+// (after cudaDeviceReset the library's module is loaded anew, at a new address).
 aph_status scratch_for_current_device(unsigned long long **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "estimate_timestep_noalloc");
   if (dev < 0 || dev >= kMaxDevices) return fail(APH_ERR_UNSUPPORTED, "device ordinal %d too large", dev);
   std::lock_guard<std::mutex> lock(g_scratch.mu);
-  if (!g_scratch.ptr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_scratch.ptr[dev] || ctx == 0 || ctx != g_scratch.ctx[dev]) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_dt_partials);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_dt_partials)");
     g_scratch.ptr[dev] = (unsigned long long *)p;
+    g_scratch.ctx[dev] = current_context_id();  // the lookup made the context current
   }
   *out = g_scratch.ptr[dev];
   return APH_OK;
@@ -123,12 +159,12 @@ extern "C" aph_status aph_hydro_estimate_timestep_noalloc(const double *prim, co
   for (int d = 0; d < 3; ++d) {
     if (d < ndim ? nx[d] < 1 : nx[d] != 1) return fail(APH_ERR_INVALID, "nx%d = %d invalid", d + 1, nx[d]);
     if (!(dx[d] > 0.0)) return fail(APH_ERR_INVALID, "dx%d must be positive", d + 1);
-    cells *= nx[d];
+    cells *= nx[d];  // at most 2^20 * 2^31 after a passed check: no overflow
+    if (cells > APH_NOALLOC_MAX_CELLS)
+      return fail(APH_ERR_INVALID,
+                  "meshblock of %d x %d x %d interior cells; the allocation-free estimate takes at "
+                  "most %d", nx[0], nx[1], nx[2], APH_NOALLOC_MAX_CELLS);
   }
-  if (cells > APH_NOALLOC_MAX_CELLS)
-    return fail(APH_ERR_INVALID,
-                "meshblock has %lld interior cells; the allocation-free estimate takes at most %d",
-                cells, APH_NOALLOC_MAX_CELLS);
   if (!(gm1 > 0.0) || !(cfl > 0.0)) return fail(APH_ERR_INVALID, "gm1 and cfl must be positive");
   unsigned long long *partials = nullptr;
   if (aph_status st = scratch_for_current_device(&partials)) return st;

@@ -358,9 +358,12 @@ __host__ __device__ constexpr size_t tma_stage_offset(int recon, int n, int T, i
 }
 
 // One pass item: lines l0..l0+nl-1 of block B along DIR.  b: the block's index in the pack;
-// tma_phase: the parity of the CTA's next mbarrier phase (TMA items flip it).
+// tma_phase: the parity of the CTA's next mbarrier phase (TMA items flip it).  Returns false
+// (the same in every thread of the CTA) when a TMA wait ran out: the window is then not used,
+// the item computes and writes nothing, and the caller leaves the launch, whose status is
+// already APH_ERR_TIMEOUT and whose results are invalid.
 template <int DIR, int RECON, int RS>
-__device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0, int nl, int T,
+__device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0, int nl, int T,
                           bool constg, bool first_pass, bool last_pass, double *sm,
                           unsigned long long &dtmin, unsigned mbar, unsigned &tma_phase) {
   constexpr int G = Halo<RECON>::G;
@@ -411,8 +414,9 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
         else tma_load_5d(dst, maps + 256, mbar, pos + ng, pl + sj, 0, 0, b);
       }
     }
-    mbar_wait_bounded(mbar, tma_phase, a.ctl, a.timeout_ns);
+    const bool arrived = mbar_wait_bounded(mbar, tma_phase, a.ctl, a.timeout_ns);
     tma_phase ^= 1u;
+    if (__syncthreads_or(!arrived)) return false;
     for (int it = tid; it < nv * nl * NW; it += nth) {
       const int v = it / (nl * NW);
       const int r = it - v * nl * NW;
@@ -651,6 +655,7 @@ __device__ void pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
     }
   }
   __syncthreads();
+  return true;
 }
 
 // Refined meshes: conservation at coarse-fine faces.  Each coarse block with a finer
@@ -859,15 +864,17 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
       const int Tc = constg ? T : split_lines(T, p.nvar);
       for (int o = 0; o < nl; o += Tc) {
         const int l0 = w.y + o, nc = min(Tc, nl - o);
+        bool ok;
         if (dir == 1)
-          pass_item<1, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin, mbar,
-                                  tma_phase);
+          ok = pass_item<1, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin,
+                                       mbar, tma_phase);
         else if (dir == 2)
-          pass_item<2, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin, mbar,
-                                  tma_phase);
+          ok = pass_item<2, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin,
+                                       mbar, tma_phase);
         else
-          pass_item<3, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin, mbar,
-                                  tma_phase);
+          ok = pass_item<3, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin,
+                                       mbar, tma_phase);
+        if (!ok) return;  // a TMA wait ran out (APH_ERR_TIMEOUT is recorded)
       }
     }
     if (!last_pass && !grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;

@@ -149,15 +149,18 @@ aph_status aph_hydro_estimate_timestep_async(aph_pack pack, double *dt_dev, void
 
 /* EstimateTimestep of one meshblock that allocates no memory at all.  This entry point
  * has no counterpart in the reference.  It is for callers that must not allocate device
- * memory when they ask for a timestep: a host code whose pool allocator owns the device
- * memory, or a step being recorded into a CUDA graph (cudaMalloc cannot be captured and
- * synchronises the device).  prim and cons are the block's fields as above; the result,
- * cfl * min, goes to *dt_dev, asynchronously on stream.  Its scratch is a fixed device
- * array inside the library, one per GPU for the life of the process, sized for at most
+ * memory when they ask for a timestep: a host code whose pool allocator has taken the
+ * device memory up front (a Kokkos or Parthenon application sized to the GPU) has none
+ * left for cudaMalloc, and cudaMalloc / cudaFree inside its step would synchronise the
+ * device.  prim and cons are the block's fields as above; the result, cfl * min, goes to
+ * *dt_dev, asynchronously on stream.  Its scratch is a fixed device array inside the
+ * library, one per GPU for the life of the process, sized for at most
  * APH_NOALLOC_MAX_CELLS interior cells; larger blocks are rejected with APH_ERR_INVALID.
- * The first call on a device looks up that array's device address, so make it before any
- * stream capture.  Calls share the array: two calls that overlap on the GPU (different
- * streams, no ordering between them) race and must not be issued. */
+ * The first call on a device looks up that array's device address (again after the
+ * device's context was replaced, e.g. by cudaDeviceReset), so make the first call before
+ * any stream capture.  Every call overwrites the array, which keeps the last call's
+ * partial minima; two calls that overlap on the GPU (different streams, no ordering
+ * between them) race and must not be issued. */
 #define APH_NOALLOC_MAX_CELLS 1048576
 aph_status aph_hydro_estimate_timestep_noalloc(const double *prim, const double *cons,
                                                const int nx[3], int nghost, int ndim,

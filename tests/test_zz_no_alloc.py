@@ -1,7 +1,7 @@
 """The allocation-free timestep estimate, called through the C ABI (needs a GPU).
 
 aph_hydro_estimate_timestep_noalloc serves callers that may not allocate device memory
-(a pool allocator owns it, or a CUDA graph is being captured).  Two calls in a row must
+(a pool allocator has taken it up front, and an allocation mid-step would synchronise).  Two calls in a row must
 agree with the regular aph_hydro_estimate_timestep on the same meshblock, within the
 fast-mode tolerance of the parity tests, and blocks above the stated maximum are refused.
 This file is collected last so that a run that stops at the first failure has already run
@@ -57,6 +57,12 @@ def test_noalloc_rejects_blocks_above_the_maximum(cuda):
     dx = (ctypes.c_double * 3)(*cfg.dx)
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     lib = _capi.load()
+    st = lib.aph_hydro_estimate_timestep_noalloc(
+        ctypes.c_void_p(md.prim[0].data_ptr()), ctypes.c_void_p(md.cons[0].data_ptr()), nx, 4, 3,
+        dx, cfg.gm1, cfg.cfl, ctypes.c_void_p(out.data_ptr()), hydro.stream_handle())
+    assert st == 1 and b"at most" in lib.aph_last_error()
+    # extents whose product would overflow 64 bits are refused too
+    nx = (ctypes.c_int * 3)(2 ** 31 - 1, 2 ** 31 - 1, 2 ** 31 - 1)
     st = lib.aph_hydro_estimate_timestep_noalloc(
         ctypes.c_void_p(md.prim[0].data_ptr()), ctypes.c_void_p(md.cons[0].data_ptr()), nx, 4, 3,
         dx, cfg.gm1, cfg.cfl, ctypes.c_void_p(out.data_ptr()), hydro.stream_handle())

@@ -2,7 +2,7 @@
 taped reference gradient of the adjoint tests (test infrastructure only).
 
 It follows the same formulas as the CUDA fast path: ConsToPrim, PPM (ppm_simple.hpp:32-161),
-PLM (plm_simple.hpp:15-32) or donor cell, HLLE (hydro_hlle.hpp:28-133) or HLLC (hydro_hllc.hpp:161-282) with the
+PLM (plm_simple.hpp:15-32) or donor cell, HLLE (hydro_hlle.hpp:28-133) or HLLC (hydro_hllc.hpp:14-146) with the
 c-limited sound speed written as sqrt(C^2 gamma p / (p (1 + 1/gm1) + rho C^2)), the flux
 divergence and the low-storage RK stages.  torch.autograd differentiates it.
 """
