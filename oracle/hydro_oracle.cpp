@@ -311,7 +311,7 @@ static void solve_hlle(const Real *wli, const Real *wri, Real gl0, Real gl1, Rea
   for (int n = 0; n < NHYDRO; ++n) flxi[n] = 0.5 * (fl[n] + fr[n]) + (fl[n] - fr[n]) * tmp;
 }
 
-// hydro_hllc.hpp:161-282 and hydro_lhllc.hpp:25-156 (low_mach selects the latter)
+// hydro_hllc.hpp:14-146 and hydro_lhllc.hpp:25-156 (low_mach selects the latter)
 static void solve_hllc(const Real *wli, const Real *wri, Real gl0, Real gl1, Real gr0,
                        Real gr1, bool low_mach, Real *flxi) {
   Real fl[NHYDRO], fr[NHYDRO];
@@ -983,6 +983,14 @@ void orc_apply_gravity(double *cons, const double *prim, int nvar, int nx1, int 
 void orc_plm(double a, double b, double c, double *ql_ip1, double *qr_i) { PLM(a, b, c, *ql_ip1, *qr_i); }
 void orc_ppm(double a, double b, double c, double e, double f, double *ql_ip1, double *qr_i) {
   PPM(a, b, c, e, f, *ql_ip1, *qr_i);
+}
+// n stencils at once: q (n, 3) or (n, 5) -> out (n, 2) = (ql_{i+1}, qr_i)
+void orc_plm_many(const double *q, double *out, long n) {
+  for (long s = 0; s < n; ++s) PLM(q[3 * s], q[3 * s + 1], q[3 * s + 2], out[2 * s], out[2 * s + 1]);
+}
+void orc_ppm_many(const double *q, double *out, long n) {
+  for (long s = 0; s < n; ++s)
+    PPM(q[5 * s], q[5 * s + 1], q[5 * s + 2], q[5 * s + 3], q[5 * s + 4], out[2 * s], out[2 * s + 1]);
 }
 // wl, wr: (rho, vx, vy, vz, p) with vx the face-normal velocity; g*: (gamma_c, gamma_e)
 void orc_riemann(int rsolver, const double *wl, const double *wr, const double *gl,

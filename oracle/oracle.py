@@ -107,6 +107,22 @@ def ppm(a, b, c, d, e):
     return l.value, r.value
 
 
+def plm_many(q):
+    """PLM of the stencils q (n, 3): (n, 2) array of (ql_{i+1}, qr_i)."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    out = np.empty((q.shape[0], 2))
+    lib().orc_plm_many(_p(q), _p(out), ctypes.c_long(q.shape[0]))
+    return out
+
+
+def ppm_many(q):
+    """PPM of the stencils q (n, 5): (n, 2) array of (ql_{i+1}, qr_i)."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    out = np.empty((q.shape[0], 2))
+    lib().orc_ppm_many(_p(q), _p(out), ctypes.c_long(q.shape[0]))
+    return out
+
+
 def riemann(rsolver, wl, wr, gl, gr):
     out = np.zeros(5)
     arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (wl, wr, gl, gr)]
