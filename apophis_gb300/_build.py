@@ -34,6 +34,7 @@ UNITS = {
     "aph_adjoint.cu": [],
     "aph_noalloc.cu": [],
     "aph_history.cu": [],
+    "aph_diag.cu": ["--fmad=false"],
 }
 
 

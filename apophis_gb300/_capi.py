@@ -7,6 +7,7 @@ from . import _build
 _LIB = None
 
 APH_OK = 0
+APH_STAGE_GHOSTS_GIVEN = 1
 STATUS_NAMES = {0: "APH_OK", 1: "APH_ERR_INVALID", 2: "APH_ERR_UNSUPPORTED", 3: "APH_ERR_CUDA",
                 4: "APH_ERR_TIMEOUT", 5: "APH_ERR_STATE"}
 RECON = {"dc": 1, "plm": 2, "ppm": 3}
@@ -20,7 +21,8 @@ _dp = ctypes.POINTER(ctypes.c_double)
 class aph_block(ctypes.Structure):
     _fields_ = [("cons", ctypes.c_void_p), ("prim", ctypes.c_void_p), ("gamma", ctypes.c_void_p),
                 ("u1", ctypes.c_void_p), ("flux", ctypes.c_void_p * 3),
-                ("nx", ctypes.c_int * 3), ("dx", ctypes.c_double * 3)]
+                ("nx", ctypes.c_int * 3), ("dx", ctypes.c_double * 3),
+                ("flux_stride", (ctypes.c_longlong * 3) * 3), ("eos_lambda", ctypes.c_void_p)]
 
 
 class aph_hydro_params(ctypes.Structure):
@@ -130,6 +132,12 @@ SIGNATURES = {
     "aph_stepper_set_clock": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                ctypes.c_void_p], ctypes.c_int),
     "aph_diag_barrier_timeout": ([ctypes.c_double, ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_stage": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
+                          ctypes.c_int),
+    "aph_stepper_local_dt": ([ctypes.c_void_p, _dp, ctypes.c_void_p], ctypes.c_int),
+    "aph_stepper_end_step": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p], ctypes.c_int),
+    "aph_diag_exact_ops": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
+                            ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_member_status": ([ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int),
                                    ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_get_config": ([ctypes.c_void_p, ctypes.POINTER(aph_stepper_config)],

@@ -473,6 +473,10 @@ struct aph_adjoint_s {
   int ckpt_every = 0;
   double *ckpts = nullptr;
   int nckpt = 0;
+  // the reverse sweep's segment storage (stage-input primitives of every step of one
+  // checkpoint segment), sized by the rollout that recorded the checkpoints
+  double *seg = nullptr;
+  size_t seg_len = 0;
 };
 
 namespace {
@@ -576,7 +580,7 @@ aph_status step_vjp_kept(aph_adjoint A, const double *kept, const double *dt_dev
 void adj_free(aph_adjoint A) {
   if (A->st) aph_stepper_destroy(A->st);
   A->st = nullptr;
-  double *bufs[] = {A->x, A->lam_w, A->lam_u, A->a, A->acc, A->states, A->ckpts, A->d_dts};
+  double *bufs[] = {A->x, A->lam_w, A->lam_u, A->a, A->acc, A->states, A->ckpts, A->d_dts, A->seg};
   for (double *p : bufs) cudaFree(p);
   cudaFree(A->d_blk);
   cudaFree(A->d_mem);
@@ -800,6 +804,17 @@ aph_status aph_adjoint_forward_members(aph_adjoint A, const double *u0, int nste
   const size_t nm = A->nmembers;
   A->nsteps = 0;
   if (aph_status st = ensure_dts(A, (size_t)nsteps * nm + nm)) return st;
+  {  // the backward sweep's segment storage, allocated here once per rollout shape
+    const size_t need = (size_t)std::min(checkpoint_every, nsteps) * stages_for(A->integrator).size() * A->n;
+    if (need > A->seg_len) {
+      cudaFree(A->seg);
+      A->seg = nullptr;
+      A->seg_len = 0;
+      cudaError_t e = cudaMalloc(&A->seg, need * sizeof(double));
+      if (e != cudaSuccess) return cuda_fail(e, "segment allocation");
+      A->seg_len = need;
+    }
+  }
   cudaError_t e = cudaMemcpyAsync(A->d_dts, dts, (size_t)nsteps * nm * sizeof(double), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // dts is the caller's host array
   if (e != cudaSuccess) return cuda_fail(e, "adjoint dt table");
@@ -851,13 +866,14 @@ aph_status aph_adjoint_backward(aph_adjoint A, const double *lam_final, double *
   const int nsteps = A->nsteps, K = A->ckpt_every;
   const size_t nm = A->nmembers;
   const int ns = (int)stages_for(A->integrator).size();
-  // segment storage: the stage-input primitives of every step of one segment, recomputed
-  // once from the segment's checkpoint
-  double *seg = nullptr;
+  // segment storage (allocated by the rollout): the stage-input primitives of every step of
+  // one segment, recomputed once from the segment's checkpoint
+  double *seg = A->seg;
   const size_t per_step = (size_t)ns * A->n;
-  cudaError_t e = cudaMalloc(&seg, (size_t)K * per_step * sizeof(double));
-  if (e != cudaSuccess) return cuda_fail(e, "segment allocation");
-  e = cudaMemcpyAsync(lam_initial, lam_final, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (!seg || (size_t)std::min(K, nsteps) * per_step > A->seg_len)
+    return fail(APH_ERR_INVALID, "no segment storage for the recorded rollout");
+  cudaError_t e =
+      cudaMemcpyAsync(lam_initial, lam_final, A->n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   aph_status st = APH_OK;
   for (int j = A->nckpt - 1; j >= 0 && st == APH_OK && e == cudaSuccess; --j) {
     const int k0 = j * K, k1 = std::min(nsteps, k0 + K);
@@ -869,7 +885,6 @@ aph_status aph_adjoint_backward(aph_adjoint A, const double *lam_final, double *
                          lam_initial, s);
   }
   if (e == cudaSuccess && st == APH_OK) e = cudaStreamSynchronize(s);
-  cudaFree(seg);
   if (st) return st;
   if (e != cudaSuccess) return cuda_fail(e, "adjoint backward");
   return check_state(A, s);

@@ -206,6 +206,7 @@ aph_status aph_pack_create(const aph_hydro_params *params, const aph_block *bloc
     B.gamma = a.gamma;
     B.u1 = a.u1;
     for (int dd = 0; dd < 3; ++dd) B.flux[dd] = a.flux[dd];
+    B.eos_lambda = a.eos_lambda;
     B.ni = a.nx[0] + 2 * d.ng;
     B.nj = d.ndim >= 2 ? a.nx[1] + 2 * d.ng : 1;
     B.nk = d.ndim >= 3 ? a.nx[2] + 2 * d.ng : 1;
@@ -213,6 +214,27 @@ aph_status aph_pack_create(const aph_hydro_params *params, const aph_block *bloc
     if (B.ncell > (1LL << 31) / 64) {
       delete p;
       return fail(APH_ERR_INVALID, "block %d too large", b);
+    }
+    for (int dd = 0; dd < 3; ++dd) {  // flux layouts: the cons shape, or the caller's strides
+      const long long *fs = a.flux_stride[dd];
+      if (fs[0] == 0 && fs[1] == 0 && fs[2] == 0) {
+        B.fs[dd][0] = B.ncell;
+        B.fs[dd][1] = (long long)B.ni * B.nj;
+        B.fs[dd][2] = B.ni;
+        continue;
+      }
+      // rows hold the faces of a cons row (one more along d), planes their rows, components
+      // their planes: every face the kernels address lies inside its own slot
+      const long long ri = B.ni + (dd == 0 ? 1 : 0);
+      const long long rj = B.nj + (dd == 1 && d.ndim >= 2 ? 1 : 0);
+      const long long rk = B.nk + (dd == 2 && d.ndim >= 3 ? 1 : 0);
+      if (fs[2] < ri || fs[1] < fs[2] * rj || fs[0] < fs[1] * rk || fs[0] > (1LL << 40)) {
+        delete p;
+        return fail(APH_ERR_INVALID,
+                    "block %d: flux[%d] strides (%lld, %lld, %lld) do not hold a (%lld, %lld, %lld) "
+                    "face array per component", b, dd, fs[0], fs[1], fs[2], rk, rj, ri);
+      }
+      for (int q = 0; q < 3; ++q) B.fs[dd][q] = fs[q];
     }
     p->max_ncell = std::max<long long>(p->max_ncell, B.ncell);
     p->max_interior = std::max(p->max_interior, a.nx[0] * a.nx[1] * a.nx[2]);

@@ -1,0 +1,38 @@
+// aph_diag.cu -- device evaluation of the exact-mode integer-pipe operations, so that tests
+// can compare them bit for bit with the IEEE operations they replace.
+#include "../../include/aph_hydro.h"
+#include "aph_capi_internal.h"
+#define APH_EXACT 1
+#include "aph_math.cuh"
+
+using namespace aph;
+
+namespace {
+
+__global__ void k_exact_ops(int op, const double *x, double *out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    double r;
+    if (op == 0) r = div6_x(v);
+    else if (op == 1) r = half_x(v);
+    else if (op == 2) r = twice_x(v);
+    else r = tame(v) ? 1.0 : 0.0;
+    out[i] = r;
+  }
+}
+
+}  // namespace
+
+extern "C" aph_status aph_diag_exact_ops(int op, const double *x, double *out, long long n,
+                                         void *stream) {
+  clear_error();
+  if (op < 0 || op > 3) return fail(APH_ERR_INVALID, "op %d not in 0..3", op);
+  if (n < 0 || (n > 0 && (!x || !out))) return fail(APH_ERR_INVALID, "NULL argument");
+  if (n == 0) return APH_OK;
+  const long long blocks = (n + 255) / 256;
+  k_exact_ops<<<(unsigned)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, (cudaStream_t)stream>>>(
+      op, x, out, n);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "diag_exact_ops");
+}

@@ -27,6 +27,8 @@ const char *amr_check(int nblocks, const AmrFaces *faces, const int (*nx)[2], in
 struct BlockDev {
   double *cons, *prim, *gamma, *u1;
   double *flux[3];
+  long long fs[3][3];   // strides of flux[d] over (n, k, j); i contiguous
+  double *eos_lambda;   // optional (3 components, the shape of cons)
   int nx[3];          // interior cells
   int ni, nj, nk;     // entire extents (ghosts included)
   int loc[3];         // logical block position in the block grid
@@ -119,6 +121,7 @@ struct StageArgs {
   int copy_u1;                  // stage 1: u1 <- u0 (interior, after the floors)
   int last;                     // last stage: dt candidates of the new state
   int init;                     // ghost fill + dt estimate only
+  int ghosts_given;             // the caller filled every ghost cell of u0: no ghost phase
   int schedule;                 // 0 strided, 1 contiguous, 2 dynamic
   unsigned long long timeout_ns;
 };

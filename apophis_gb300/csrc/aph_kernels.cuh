@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(kThreads) k_cons_to_prim(PackDev p, const Bloc
     const double di = 1.0 / u[IDN];
     for (int n = NHYDRO; n < p.nvar; ++n) B.prim[n * nc + c] = B.cons[n * nc + c] * di;
   }
+  if (B.eos_lambda && B.eos_lambda[2 * nc + c] == 0.0) B.eos_lambda[2 * nc + c] = 7.0;  // hydro.cpp:491-493
   if (fl && floor_flag) atomicOr(floor_flag, 1);
 }
 
@@ -155,7 +156,11 @@ __global__ void __launch_bounds__(kThreads) k_fluxes(PackDev p, const BlockDev *
     int i0, j0, k0, ln;
     long long s;
     line_geometry<DIR>(B, p.ndim, p.ng, line0 + t, i0, j0, k0, s, ln);
-    const long long cell = ((long long)k0 * B.nj + j0) * B.ni + i0 + (long long)f * s;
+    // face f of the line: cell (k0, j0, i0) moved f cells along DIR, in flux[DIR-1]'s layout
+    const long long* fs = B.fs[DIR - 1];
+    const long long fcell = (long long)(k0 + (DIR == 3 ? f : 0)) * fs[1] +
+                            (long long)(j0 + (DIR == 2 ? f : 0)) * fs[2] + (i0 + (DIR == 1 ? f : 0));
+    const long long fn = fs[0];
     const size_t oL = ((size_t)t) * maxP + f;      // ql_f  (from cell f-1)
     const size_t oR = ((size_t)t) * maxP + f + 1;  // qr_f  (from cell f)
     const size_t vs = (size_t)T * maxP;
@@ -166,14 +171,14 @@ __global__ void __launch_bounds__(kThreads) k_fluxes(PackDev p, const BlockDev *
     wr[IV3] = sR[ivz * vs + oR]; wr[IPR] = sR[IPR * vs + oR];
     riemann<RS, false>(wl, wr, sL[nvar * vs + oL], sL[(nvar + 1) * vs + oL],
                        sR[nvar * vs + oR], sR[(nvar + 1) * vs + oR], gc, flx);
-    flux[IDN * nc + cell] = flx[IDN];
-    flux[ivx * nc + cell] = flx[IV1];
-    flux[ivy * nc + cell] = flx[IV2];
-    flux[ivz * nc + cell] = flx[IV3];
-    flux[IEN * nc + cell] = flx[IEN];
+    flux[IDN * fn + fcell] = flx[IDN];
+    flux[ivx * fn + fcell] = flx[IV1];
+    flux[ivy * fn + fcell] = flx[IV2];
+    flux[ivz * fn + fcell] = flx[IV3];
+    flux[IEN * fn + fcell] = flx[IEN];
     // passive scalars: upwind by the mass flux (hydro.cpp:607-615)
     for (int v = NHYDRO; v < nvar; ++v)
-      flux[v * nc + cell] = flx[IDN] * (!is_neg(flx[IDN]) ? sL[v * vs + oL] : sR[v * vs + oR]);
+      flux[v * fn + fcell] = flx[IDN] * (!is_neg(flx[IDN]) ? sL[v * vs + oL] : sR[v * vs + oR]);
   }
 }
 
@@ -181,13 +186,20 @@ __global__ void __launch_bounds__(kThreads) k_fluxes(PackDev p, const BlockDev *
 // UpdateWithFluxDivergence over the interior: u0 = gam0 u0 + gam1 u1 + beta_dt (-div F)
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ bool interior_cell(const BlockDev &B, int ndim, int ng, int idx,
-                                              long long &cell) {
+                                              long long &cell, int &ci, int &cj, int &ck) {
   const int n0 = B.nx[0], n1 = B.nx[1], n2 = B.nx[2];
   if (idx >= n0 * n1 * n2) return false;
   const int i = idx % n0, j = (idx / n0) % n1, k = idx / (n0 * n1);
   const int si = ng, sj = dim_start(1, ndim, ng), sk = dim_start(2, ndim, ng);
-  cell = ((long long)(k + sk) * B.nj + (j + sj)) * B.ni + (i + si);
+  ci = i + si;
+  cj = j + sj;
+  ck = k + sk;
+  cell = ((long long)ck * B.nj + cj) * B.ni + ci;
   return true;
+}
+// Index of face (k, j, i) of component n in flux[d] (face i on the low side of cell i).
+__device__ __forceinline__ long long flux_index(const BlockDev &B, int d, int n, int k, int j, int i) {
+  return n * B.fs[d][0] + k * B.fs[d][1] + j * B.fs[d][2] + i;
 }
 
 __global__ void __launch_bounds__(kThreads) k_update(PackDev p, const BlockDev *blocks,
@@ -195,20 +207,34 @@ __global__ void __launch_bounds__(kThreads) k_update(PackDev p, const BlockDev *
                                                      double beta_dt_host, const double *dt_dev) {
   const BlockDev &B = blocks[p.block0 + blockIdx.y];
   long long c;
-  if (!interior_cell(B, p.ndim, p.ng, blockIdx.x * blockDim.x + threadIdx.x, c)) return;
+  int ci, cj, ck;
+  if (!interior_cell(B, p.ndim, p.ng, blockIdx.x * blockDim.x + threadIdx.x, c, ci, cj, ck)) return;
   const double beta_dt = dt_dev ? beta * dt_dev[0] : beta_dt_host;
   const double a1 = B.dx[1] * B.dx[2], a2 = B.dx[0] * B.dx[2], a3 = B.dx[0] * B.dx[1];
   const double vol = B.dx[0] * B.dx[1] * B.dx[2];
   const long long nc = B.ncell;
-  const long long sj = B.ni, sk = (long long)B.ni * B.nj;
   for (int n = 0; n < p.nvar; ++n) {
     const long long q = n * nc + c;
-    double du = (a1 * B.flux[0][q + 1] - a1 * B.flux[0][q]);
-    if (p.ndim >= 2) du += (a2 * B.flux[1][q + sj] - a2 * B.flux[1][q]);
-    if (p.ndim == 3) du += (a3 * B.flux[2][q + sk] - a3 * B.flux[2][q]);
+    const long long f1 = flux_index(B, 0, n, ck, cj, ci);
+    double du = (a1 * B.flux[0][f1 + 1] - a1 * B.flux[0][f1]);
+    if (p.ndim >= 2) {
+      const long long f2 = flux_index(B, 1, n, ck, cj, ci);
+      du += (a2 * B.flux[1][f2 + B.fs[1][2]] - a2 * B.flux[1][f2]);
+    }
+    if (p.ndim == 3) {
+      const long long f3 = flux_index(B, 2, n, ck, cj, ci);
+      du += (a3 * B.flux[2][f3 + B.fs[2][1]] - a3 * B.flux[2][f3]);
+    }
     const double div = -du / vol;
     B.cons[q] = gam0 * B.cons[q] + gam1 * B.u1[q] + beta_dt * div;
   }
+}
+
+// Face (a along d, t across) of component n of flux[d] of a 2D block (as amr_cell).
+__device__ __forceinline__ long long amr_face(const BlockDev &B, int ng, int d, int n, int a, int t) {
+  const int i = d == 0 ? ng + a : ng + t;
+  const int j = d == 0 ? ng + t : ng + a;
+  return flux_index(B, d, n, 0, j, i);
 }
 
 // Refined 2D meshes: the same update with the coarse-fine correction of each coarse
@@ -218,8 +244,9 @@ __global__ void __launch_bounds__(kThreads) k_update_amr(PackDev p, const BlockD
                                                          double beta_dt_host, const double *dt_dev) {
   const BlockDev &B = blocks[p.block0 + blockIdx.y];
   long long c;
+  int ci, cj, ck;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!interior_cell(B, p.ndim, p.ng, idx, c)) return;
+  if (!interior_cell(B, p.ndim, p.ng, idx, c, ci, cj, ck)) return;
   const int ii = idx % B.nx[0], jj = idx / B.nx[0];
   const double beta_dt = dt_dev ? beta * dt_dev[0] : beta_dt_host;
   const double a1 = B.dx[1] * B.dx[2], a2 = B.dx[0] * B.dx[2];
@@ -227,8 +254,9 @@ __global__ void __launch_bounds__(kThreads) k_update_amr(PackDev p, const BlockD
   const long long nc = B.ncell;
   for (int n = 0; n < p.nvar; ++n) {
     const long long q = n * nc + c;
-    double du = (a1 * B.flux[0][q + 1] - a1 * B.flux[0][q]);
-    du += (a2 * B.flux[1][q + B.ni] - a2 * B.flux[1][q]);
+    const long long f1 = flux_index(B, 0, n, 0, cj, ci), f2 = flux_index(B, 1, n, 0, cj, ci);
+    double du = (a1 * B.flux[0][f1 + 1] - a1 * B.flux[0][f1]);
+    du += (a2 * B.flux[1][f2 + B.fs[1][2]] - a2 * B.flux[1][f2]);
     for (int face = 0; face < 4; ++face) {
       if (B.amr.kind[face] != FACE_FINER) continue;
       const int d = face / 2, s = face % 2, td = 1 - d;
@@ -238,12 +266,12 @@ __global__ void __launch_bounds__(kThreads) k_update_amr(PackDev p, const BlockD
       const int tg2 = 2 * (B.amr.origin[td] + t);
       const BlockDev &F = amr_fine_nbr(blocks, B, face, td, tg2);
       const int ft = tg2 - F.amr.origin[td];
-      const long long fo = n * B.ncell + amr_cell(B, p.ng, d, s == 0 ? 0 : B.nx[d], t);
+      const long long fo = amr_face(B, p.ng, d, n, s == 0 ? 0 : B.nx[d], t);
       const int ffa = s == 0 ? F.nx[d] : 0;
-      const long long f0 = n * F.ncell + amr_cell(F, p.ng, d, ffa, ft);
-      const long long f1 = n * F.ncell + amr_cell(F, p.ng, d, ffa, ft + 1);
+      const long long g0 = amr_face(F, p.ng, d, n, ffa, ft);
+      const long long g1 = amr_face(F, p.ng, d, n, ffa, ft + 1);
       const double Fold = B.flux[d][fo];
-      const double Fnew = 0.5 * (F.flux[d][f0] + F.flux[d][f1]);
+      const double Fnew = 0.5 * (F.flux[d][g0] + F.flux[d][g1]);
       du = s == 0 ? du + (area * Fold - area * Fnew) : du + (area * Fnew - area * Fold);
     }
     const double div = -du / vol;
@@ -281,7 +309,8 @@ __global__ void __launch_bounds__(kThreads) k_estimate_dt(PackDev p, const Block
   const BlockDev &B = blocks[p.block0 + blockIdx.y];
   long long c;
   unsigned long long v = ~0ULL;
-  if (interior_cell(B, p.ndim, p.ng, blockIdx.x * blockDim.x + threadIdx.x, c)) {
+  int ci, cj, ck;
+  if (interior_cell(B, p.ndim, p.ng, blockIdx.x * blockDim.x + threadIdx.x, c, ci, cj, ck)) {
     const long long nc = B.ncell;
     double w[NHYDRO];
 #pragma unroll
@@ -304,7 +333,8 @@ __global__ void __launch_bounds__(kThreads) k_apply_gravity(PackDev p, const Blo
                                                             const double *dt_dev) {
   const BlockDev &B = blocks[p.block0 + blockIdx.y];
   long long c;
-  if (!interior_cell(B, p.ndim, p.ng, blockIdx.x * blockDim.x + threadIdx.x, c)) return;
+  int ci, cj, ck;
+  if (!interior_cell(B, p.ndim, p.ng, blockIdx.x * blockDim.x + threadIdx.x, c, ci, cj, ck)) return;
   const double dt = dt_dev ? beta * dt_dev[0] : beta_dt_host;
   const long long nc = B.ncell;
   const double rho = B.prim[IDN * nc + c];

@@ -83,6 +83,46 @@ __device__ __forceinline__ bool strictly_outside(double x, double a, double b) {
   return (kx > ka && kx > kb) || (kx < ka && kx < kb);
 }
 
+// ---- exact operations on the integer pipe for tame operands -------------------------
+// A value is tame when it is zero or a normal number with 2^-200 <= |x| < 2^201.  The
+// reconstruction of a window of tame values only forms sums, differences and a few
+// products and quotients of them, which stay zero or normal far from the underflow and
+// overflow thresholds (a nonzero difference of tame values is at least 2^-252).  For those
+// values the operations below give exactly the bits of the FP64 operation they replace:
+//   half_x(x) == 0.5 * x and twice_x(x) == 2.0 * x (an exponent step; zero kept),
+//   div6_x(x) == x / 6.0 (correctly rounded, see below),
+// and the sign of a product of two differences is the product of their signs (no product
+// underflows), which strictly_between / strictly_outside decide on the integer pipe.
+__device__ __forceinline__ bool tame(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
+  const unsigned e = hi >> 20;  // biased exponent
+  return (e - (1023u - 200u) <= 400u) || ((hi | (unsigned)__double2loint(x)) == 0u);
+}
+__device__ __forceinline__ double half_x(double x) {
+  const long long b = __double_as_longlong(x);
+  return (b << 1) == 0 ? x : __longlong_as_double(b - (1LL << 52));
+}
+__device__ __forceinline__ double twice_x(double x) {
+  const long long b = __double_as_longlong(x);
+  return (b << 1) == 0 ? x : __longlong_as_double(b + (1LL << 52));
+}
+// x / 6.0 correctly rounded, by the exact remainder (the method of Brisebarre, Muller and
+// Raina for a divisor known in advance, with the rounding decided by comparing remainders):
+// c = RN(1/6) has relative error exactly 2^-54, so q0 = RN(x c) is within one ulp of x/6
+// (faithful); then r0 = x - 6 q0 is exact (one fma), x/6 lies strictly between q0 and its
+// neighbour q1 on the side of r0's sign, r1 = x - 6 q1 is exact too, and the nearer of q0 and
+// q1 -- the one with the smaller remainder -- is RN(x/6) (a tie would need x to have more
+// than 53 significant bits).  Valid for x zero or normal with 2^-1000 < |x| < 2^1000.
+__device__ __forceinline__ double div6_x(double x) {
+  const double q0 = x * (1.0 / 6.0);
+  const double r0 = fma(-6.0, q0, x);
+  const long long b = __double_as_longlong(q0);
+  const long long b1 = b + ((is_pos(r0) == is_pos(q0)) ? 1LL : -1LL);  // toward x/6 (q0 != 0)
+  const double q1 = __longlong_as_double(b1);
+  const double r1 = fma(-6.0, q1, x);
+  return ((b << 1) != 0 && mag(r1) < mag(r0)) ? q1 : q0;
+}
+
 // ---- gamma-dependent constants of a pack (fast mode) ---------------------------
 struct GasConsts {
   double gm1, igm1, gamma;      // eos/gm1, 1/gm1, gm1+1
@@ -116,17 +156,18 @@ __device__ __forceinline__ bool cons_to_prim_tail(double *u, double *w, double &
   const double e_k = __dmul_rn(__dmul_rn(0.5, di),
                                __dadd_rn(__dadd_rn(__dmul_rn(m1, m1), __dmul_rn(m2, m2)), __dmul_rn(m3, m3)));
   double u_e = u[IEN];
-  double w_p = __dmul_rn(__dmul_rn(gm1, u_d), __ddiv_rn(__dsub_rn(u_e, e_k), u_d));
+  double sie = __ddiv_rn(__dsub_rn(u_e, e_k), u_d);  // (u_e - e_k) / u_d
+  double w_p = __dmul_rn(__dmul_rn(gm1, u_d), sie);
   w_p = is_neg(w_p) ? 0.0 : w_p;  // eos_pressure
   const bool floored = !gt(w_p, pfloor);
   if (floored) {
     const double gm1q = __ddiv_rn(w_p, __dmul_rn(u_d, e_k));  // hydro.cpp:517
     u_e = __dadd_rn(__ddiv_rn(pfloor, gm1q), e_k);
     w_p = pfloor;
+    sie = __ddiv_rn(__dsub_rn(u_e, e_k), u_d);  // of the floored energy (unchanged otherwise)
   }
   u[IEN] = u_e;
   w[IPR] = w_p;
-  const double sie = __ddiv_rn(__dsub_rn(u_e, e_k), u_d);
   const double small = 10.0 * 2.2250738585072014e-308;
   double b = __dmul_rn(__dmul_rn(__dmul_rn(gm1, __dadd_rn(gm1, 1.0)), u_d), sie);  // eos_bulk_modulus
   b = lt(small, b) ? b : small;
@@ -143,7 +184,7 @@ __device__ __forceinline__ bool cons_to_prim_cell(double *u, double *w, double &
   double u_d = u[IDN];
   u_d = gt(u_d, dfloor) ? u_d : dfloor;
   u[IDN] = u_d;
-  const double di = 1.0 / u_d;
+  const double di = __drcp_rn(u_d);  // the correctly rounded 1.0 / u_d
   w[IDN] = u_d;
   w[IV1] = u[IM1] * di;
   w[IV2] = u[IM2] * di;
@@ -193,20 +234,47 @@ __device__ __forceinline__ void plm(double q_im1, double q_i, double q_ip1, doub
 // PPM(q_im2..q_ip2) of ppm_simple.hpp:32-161.
 //
 // dd(c) = 0.5*(q[c+1]-q[c]) + 0.5*(q[c]-q[c-1]);  d2(c) = (q[c-1]+q[c+1]) - 2*q[c]
+//
+// TAME (exact mode, every window value tame): the same bits with the scalings by 2, 1/2
+// and 1/6 and the sign tests of products of differences on the integer pipe.
+template <bool TAME = false>
 __device__ __forceinline__ double ppm_dd(double qm1, double q0, double qp1) {
 #if APH_EXACT
+  if (TAME) return half_x(qp1 - q0) + half_x(q0 - qm1);
   return 0.5 * (qp1 - q0) + 0.5 * (q0 - qm1);
 #else
   return 0.5 * (qp1 - qm1);  // the same quantity with one rounding
 #endif
 }
+template <bool TAME = false>
 __device__ __forceinline__ double ppm_d2(double qm1, double q0, double qp1) {
+  if (APH_EXACT && TAME) return (qm1 + qp1) - twice_x(q0);
   return (qm1 + qp1) - 2.0 * q0;
 }
 // Face between cells c-1 (value qm1) and c (value q0): ddm1 = dd(c-1), dd0 = dd(c),
 // d2m1 = d2(c-1), d20 = d2(c).
+template <bool TAME = false>
 __device__ __forceinline__ double ppm_face(double qm1, double q0, double ddm1, double dd0,
                                            double d2m1, double d20) {
+#if APH_EXACT
+  if (TAME) {
+    const double s = qm1 + q0;
+    const double avg = half_x(s);
+    double dph = avg + div6_x(ddm1 - dd0);
+    const double qa = 3.0 * (s - twice_x(dph));
+    double qd = 0.0;
+    const bool sa = is_neg(qa);
+    if (sa == is_neg(d2m1) && sa == is_neg(d20)) {
+      const unsigned long long mb = mag(d2m1), mc = mag(d20);
+      const double m = PPM_C2 * from_bits(mc < mb ? mc : mb);
+      const unsigned long long mm = mag(m), ma = mag(qa);
+      qd = flip_if(from_bits(ma < mm ? ma : mm), sa);
+    }
+    // (dph - qm1) * (q0 - dph) < 0, the differences being nonzero and their product normal
+    if (strictly_outside(dph, qm1, q0)) dph = avg - div6_x(qd);
+    return dph;
+  }
+#endif
   const double avg = 0.5 * (qm1 + q0);
 #if APH_EXACT
   double dph = avg + (ddm1 - dd0) / 6.0;
@@ -238,18 +306,26 @@ __device__ __forceinline__ double ppm_face(double qm1, double q0, double ddm1, d
 
 // Cell limiter: dph_lo, dph_hi are the limited values at faces i-1/2, i+1/2.
 // Outputs ql_ip1 (left state of face i+1/2) and qr_i (right state of face i-1/2).
+template <bool TAME = false>
 __device__ __forceinline__ void ppm_cell(double q_im2, double q_im1, double q_i, double q_ip1,
                                          double q_ip2, double d2m1, double d20, double d2p1,
                                          double dph_lo, double dph_hi, double &ql_ip1,
                                          double &qr_i) {
-  const double d2qf = 6.0 * (dph_lo + dph_hi - 2.0 * q_i);
+  constexpr bool T = APH_EXACT && TAME;
+  const double d2qf = 6.0 * (dph_lo + dph_hi - (T ? twice_x(q_i) : 2.0 * q_i));
   double qr = dph_lo, ql = dph_hi;
   const double dqf_minus = q_i - qr;
   const double dqf_plus = ql - q_i;
 #if APH_EXACT
-  const double qa_tmp = dqf_minus * dqf_plus;
-  const double qb_tmp = (q_ip1 - q_i) * (q_i - q_im1);
-  if (!is_pos(qa_tmp) || !is_pos(qb_tmp)) {
+  bool extremum;
+  if (T) {  // the two products' signs, as in ppm_face
+    extremum = !strictly_between(qr, q_i, ql) || !strictly_between(q_im1, q_i, q_ip1);
+  } else {
+    const double qa_tmp = dqf_minus * dqf_plus;
+    const double qb_tmp = (q_ip1 - q_i) * (q_i - q_im1);
+    extremum = !is_pos(qa_tmp) || !is_pos(qb_tmp);
+  }
+  if (extremum) {
 #else
   if (!strictly_between(qr, q_i, ql) || !strictly_between(q_im1, q_i, q_ip1)) {
 #endif
@@ -282,8 +358,8 @@ __device__ __forceinline__ void ppm_cell(double q_im2, double q_im1, double q_i,
 #endif
     }
   } else {
-    if (mag(dqf_minus) >= twice_mag(dqf_plus)) qr = q_i - 2.0 * dqf_plus;
-    if (mag(dqf_plus) >= twice_mag(dqf_minus)) ql = q_i + 2.0 * dqf_minus;
+    if (mag(dqf_minus) >= twice_mag(dqf_plus)) qr = q_i - (T ? twice_x(dqf_plus) : 2.0 * dqf_plus);
+    if (mag(dqf_plus) >= twice_mag(dqf_minus)) ql = q_i + (T ? twice_x(dqf_minus) : 2.0 * dqf_minus);
   }
   ql_ip1 = ql;
   qr_i = qr;
@@ -344,8 +420,8 @@ __device__ __forceinline__ void solve_hlle(const double *wli, const double *wri,
   if (CONSTG) {
     igm1l = igm1r = gc.igm1;
   } else {
-    igm1l = 1.0 / (gle - 1);
-    igm1r = 1.0 / (gre - 1);
+    igm1l = __drcp_rn(gle - 1);  // the correctly rounded 1.0 / (gle - 1), cheaper than a division
+    igm1r = __drcp_rn(gre - 1);
   }
   const double cl = sound_speed<CONSTG>(wli[IDN], wli[IPR], gammal, igm1l, gc);
   const double cr = sound_speed<CONSTG>(wri[IDN], wri[IPR], gammar, igm1r, gc);
@@ -398,6 +474,127 @@ __device__ __forceinline__ void solve_hlle(const double *wli, const double *wri,
   for (int n = 0; n < NHYDRO; ++n) flxi[n] = 0.5 * (fl[n] + fr[n]) + (fl[n] - fr[n]) * tmp;
 }
 
+// x = 2^k with x and 1/x both normal: then y / x == y * (1/x) exactly for every y (both are
+// the correctly rounded y * 2^-k), so a division by x is a multiplication.
+__device__ __forceinline__ bool pow2_normal(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long e = b >> 52;  // the sign bit must be 0
+  return (b & 0xfffffffffffffULL) == 0 && e >= 1 && e <= 2045;
+}
+// y / vol, correctly rounded; ivol = 1 / vol, p2 = pow2_normal(vol) (uniform over a block)
+__device__ __forceinline__ double div_vol(double y, double vol, double ivol, bool p2) {
+  if (p2) return y * ivol;
+  return y / vol;
+}
+
+// exponent field all ones: an infinity or a NaN
+__device__ __forceinline__ bool nonfinite(double x) {
+  return ((__double2hiint(x) >> 20) & 0x7ff) == 0x7ff;
+}
+
+// HLLC in the exact mode with the reference's roundings (hydro_hllc.hpp:45-145, and the
+// low-Mach pstar of hydro_lhllc.hpp:71-79), arranged for the GPU without changing a bit:
+//  * the shock factor (gamma_l + 1) / (2 gamma_r), which the reference writes identically
+//    for both sides, is formed once, and a face shocked on one side only takes one
+//    division and square root whichever side it is;
+//  * the contact branch picks its operands instead of its code, so both branches are the
+//    same two divisions: ul = sstar / (sstar - bm), ustar = -bm / (sstar - bm) when
+//    sstar >= 0, else ur = -sstar / (bp - sstar), ustar = bp / (bp - sstar);
+//  * TAME (the reconstruction window was tame): the flux is formed from the upwind side only.
+//    The reference's ul*fl + ur*fr has one weight exactly 0, and RN(a + (+-0)) == a for a
+//    nonzero a, so the other side's term (0 * f, a signed zero: no product of values derived
+//    from a tame window overflows) is added, in the reference's order, only where the upwind
+//    term is zero and the sign of the zero sum depends on it, or where the other side is
+//    not finite.  The halvings and doublings run on the integer pipe (half_x, twice_x).
+//    Without TAME both sides' terms are always formed.
+template <bool LOWMACH, bool TAME>
+__device__ __forceinline__ void solve_hllc_exact(const double *wli, const double *wri, double glc,
+                                                 double gle, double grc, double gre, double *flxi) {
+  auto hlf = [](double x) { return TAME ? half_x(x) : 0.5 * x; };
+  const double gammal = glc, gammar = grc;
+  const double igm1l = __drcp_rn(gle - 1), igm1r = __drcp_rn(gre - 1);  // == 1.0 / (g - 1)
+  const double cl = C_LIGHT * sqrt(gammal / (1 + (igm1l + wli[IDN] * C_LIGHT2 / wli[IPR])));
+  const double cr = C_LIGHT * sqrt(gammar / (1 + (igm1r + wri[IDN] * C_LIGHT2 / wri[IPR])));
+  const double rhoa = hlf(wli[IDN] + wri[IDN]);
+  const double ca = hlf(cl + cr);
+  double pstar;
+  if (!LOWMACH) {
+    pstar = hlf(wli[IPR] + wri[IPR]) - hlf(wri[IV1] - wli[IV1]) * rhoa * ca;
+  } else {
+    const double machl = sqrt(wli[IV1] * wli[IV1] + wli[IV2] * wli[IV2] + wli[IV3] * wli[IV3]);
+    const double machr = sqrt(wri[IV1] * wri[IV1] + wri[IV2] * wri[IV2] + wri[IV3] * wri[IV3]);
+    const double chi = smax(machl, machr);
+    const double phi = chi * (2.0 - chi);
+    pstar = hlf(wli[IPR] + wri[IPR]) - hlf(wri[IV1] - wli[IV1]) * rhoa * ca * phi;
+  }
+  double ql = 1.0, qr = 1.0;
+  const bool bl = gt(pstar, wli[IPR]), br = gt(pstar, wri[IPR]);
+  if (bl || br) {
+    const double k = (gammal + 1) / (TAME ? twice_x(gammar) : 2 * gammar);
+    const double q1 = sqrt(1.0 + k * (pstar / (bl ? wli[IPR] : wri[IPR]) - 1.0));
+    if (bl) ql = q1;
+    else qr = q1;
+    if (bl && br) qr = sqrt(1.0 + k * (pstar / wri[IPR] - 1.0));
+  }
+  const double sl = wli[IV1] - cl * ql;
+  const double sr = wri[IV1] + cr * qr;
+  const double bp = is_pos(sr) ? sr : TINY_NUMBER;
+  const double bm = is_neg(sl) ? sl : -TINY_NUMBER;
+  const double vxl0 = wli[IV1] - sl;
+  const double vxr0 = wri[IV1] - sr;
+  const double tl = wli[IPR] + vxl0 * wli[IDN] * wli[IV1];
+  const double tr = wri[IPR] + vxr0 * wri[IDN] * wri[IV1];
+  const double ml = wli[IDN] * vxl0;
+  const double mr = -(wri[IDN] * vxr0);
+  const double sstar = (tl - tr) / (ml + mr);
+  double cp = (ml * tr + mr * tl) / (ml + mr);
+  cp = is_pos(cp) ? cp : 0.0;
+  const bool L = !is_neg(sstar);  // sstar >= 0.0
+  const double den = L ? sstar - bm : bp - sstar;
+  const double coef = (L ? sstar : -sstar) / den;  // ul, or ur
+  const double ustar = (L ? -bm : bp) / den;
+  // the upwind side (U) and the other one (O)
+  const double *wu = L ? wli : wri, *wo = L ? wri : wli;
+  const double igu = L ? igm1l : igm1r;
+  const double bu = L ? bm : bp, bo = L ? bp : bm;
+  const double vx = wu[IV1] - bu;
+  double f[NHYDRO];
+  f[IDN] = wu[IDN] * vx;
+  f[IV1] = wu[IDN] * wu[IV1] * vx + wu[IPR];
+  f[IV2] = wu[IDN] * wu[IV2] * vx;
+  f[IV3] = wu[IDN] * wu[IV3] * vx;
+  const double eu = wu[IPR] * igu + hlf(wu[IDN]) * (wu[IV1] * wu[IV1] + wu[IV2] * wu[IV2] + wu[IV3] * wu[IV3]);
+  f[IEN] = eu * vx + wu[IPR] * wu[IV1];
+  const bool obad = nonfinite(wo[IDN]) || nonfinite(wo[IV1]) || nonfinite(wo[IV2]) ||
+                    nonfinite(wo[IV3]) || nonfinite(wo[IPR]) || nonfinite(bo) ||
+                    nonfinite(L ? igm1r : igm1l);
+  double t[NHYDRO];
+#pragma unroll
+  for (int n = 0; n < NHYDRO; ++n) {
+    t[n] = coef * f[n];
+    if (!TAME || obad || (__double_as_longlong(t[n]) << 1) == 0) {  // add the reference's 0 * fo
+      const double vxo = wo[IV1] - bo;
+      double fo;
+      if (n == IDN) fo = wo[IDN] * vxo;
+      else if (n == IV1) fo = wo[IDN] * wo[IV1] * vxo + wo[IPR];
+      else if (n == IV2) fo = wo[IDN] * wo[IV2] * vxo;
+      else if (n == IV3) fo = wo[IDN] * wo[IV3] * vxo;
+      else {
+        const double eo = wo[IPR] * (L ? igm1r : igm1l) +
+                          hlf(wo[IDN]) * (wo[IV1] * wo[IV1] + wo[IV2] * wo[IV2] + wo[IV3] * wo[IV3]);
+        fo = eo * vxo + wo[IPR] * wo[IV1];
+      }
+      const double zo = 0.0 * fo;
+      t[n] = L ? t[n] + zo : zo + t[n];  // the reference's order: ul*fl + ur*fr
+    }
+  }
+  flxi[IDN] = t[IDN];
+  flxi[IV1] = t[IV1] + ustar * cp;
+  flxi[IV2] = t[IV2];
+  flxi[IV3] = t[IV3];
+  flxi[IEN] = t[IEN] + ustar * cp * sstar;
+}
+
 template <bool CONSTG, bool LOWMACH>
 __device__ __forceinline__ void solve_hllc(const double *wli, const double *wri, double glc,
                                            double gle, double grc, double gre,
@@ -408,8 +605,8 @@ __device__ __forceinline__ void solve_hllc(const double *wli, const double *wri,
   if (CONSTG) {
     igm1l = igm1r = gc.igm1;
   } else {
-    igm1l = 1.0 / (gle - 1);
-    igm1r = 1.0 / (gre - 1);
+    igm1l = __drcp_rn(gle - 1);  // the correctly rounded 1.0 / (gle - 1), cheaper than a division
+    igm1r = __drcp_rn(gre - 1);
   }
   const double cl = sound_speed<CONSTG>(wli[IDN], wli[IPR], gammal, igm1l, gc);
   const double cr = sound_speed<CONSTG>(wri[IDN], wri[IPR], gammar, igm1r, gc);
@@ -530,16 +727,24 @@ __device__ __forceinline__ void solve_hllc(const double *wli, const double *wri,
   flxi[IEN] = ul * fl[IEN] + ur * fr[IEN] + ustar * cp * sstar;
 }
 
-template <int RS, bool CONSTG>
+template <int RS, bool CONSTG, bool TAME = false>
 __device__ __forceinline__ void riemann(const double *wl, const double *wr, double glc, double gle,
                                         double grc, double gre, const GasConsts &gc,
                                         double *flx) {
   if (RS == RS_HLLE) {
     solve_hlle<CONSTG>(wl, wr, glc, gle, grc, gre, gc, flx);
   } else if (RS == RS_HLLC) {
+#if APH_EXACT
+    solve_hllc_exact<false, TAME>(wl, wr, glc, gle, grc, gre, flx);
+#else
     solve_hllc<CONSTG, false>(wl, wr, glc, gle, grc, gre, gc, flx);
+#endif
   } else if (RS == RS_LHLLC) {
+#if APH_EXACT
+    solve_hllc_exact<true, TAME>(wl, wr, glc, gle, grc, gre, flx);
+#else
     solve_hllc<CONSTG, true>(wl, wr, glc, gle, grc, gre, gc, flx);
+#endif
   } else {
 #pragma unroll
     for (int n = 0; n < NHYDRO; ++n) flx[n] = 0.0;

@@ -357,6 +357,52 @@ __host__ __device__ constexpr size_t tma_stage_offset(int recon, int n, int T, i
          16 * 16;
 }
 
+// PPM of a pass item's window: W holds V x T lines of cells -G..n+G-1 (row width n + 2G);
+// per cell the second differences D2 and centred differences DD (cells -2..n+1), per face
+// the limited value DPH once (faces -1..n+1), then per cell the parabola limiter writes the
+// left state of face c+1 to SL[c+1] and the right state of face c to SR[c+1] (cells -1..n).
+template <bool TAME>
+__device__ __forceinline__ void ppm_window(const double *W, double *D2, double *DD, double *DPH,
+                                           double *SL, double *SR, int V, int nl, int T, int n,
+                                           int G) {
+  const int NW = n + 2 * G;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  auto w_at = [&](int v, int t, int c) -> double { return W[((size_t)v * T + t) * NW + c + G]; };
+  const int w4 = n + 4, w3 = n + 3;
+  for (int it = tid; it < V * nl * w4; it += nth) {  // cells -2..n+1
+    const int v = it / (nl * w4);
+    const int r = it - v * nl * w4;
+    const int t = r / w4, c = r - t * w4 - 2;
+    const double qm = w_at(v, t, c - 1), q0 = w_at(v, t, c), qp = w_at(v, t, c + 1);
+    D2[((size_t)v * T + t) * w4 + c + 2] = ppm_d2<TAME>(qm, q0, qp);
+    DD[((size_t)v * T + t) * w4 + c + 2] = ppm_dd<TAME>(qm, q0, qp);
+  }
+  __syncthreads();
+  for (int it = tid; it < V * nl * w3; it += nth) {  // faces -1..n+1
+    const int v = it / (nl * w3);
+    const int r = it - v * nl * w3;
+    const int t = r / w3, f = r - t * w3 - 1;
+    const size_t o = ((size_t)v * T + t) * w4;
+    DPH[((size_t)v * T + t) * w3 + f + 1] =
+        ppm_face<TAME>(w_at(v, t, f - 1), w_at(v, t, f), DD[o + f + 1], DD[o + f + 2],
+                       D2[o + f + 1], D2[o + f + 2]);
+  }
+  __syncthreads();
+  const int w2 = n + 2;
+  for (int it = tid; it < V * nl * w2; it += nth) {  // cells -1..n
+    const int v = it / (nl * w2);
+    const int r = it - v * nl * w2;
+    const int t = r / w2, c = r - t * w2 - 1;
+    const size_t o4 = ((size_t)v * T + t) * w4, o3 = ((size_t)v * T + t) * w3;
+    double ql, qr;
+    ppm_cell<TAME>(w_at(v, t, c - 2), w_at(v, t, c - 1), w_at(v, t, c), w_at(v, t, c + 1),
+                   w_at(v, t, c + 2), D2[o4 + c + 1], D2[o4 + c + 2], D2[o4 + c + 3],
+                   DPH[o3 + c + 1], DPH[o3 + c + 2], ql, qr);
+    SL[((size_t)v * T + t) * w2 + c + 1] = ql;
+    SR[((size_t)v * T + t) * w2 + c + 1] = qr;
+  }
+}
+
 // One pass item: lines l0..l0+nl-1 of block B along DIR.  b: the block's index in the pack;
 // tma_phase: the parity of the CTA's next mbarrier phase (TMA items flip it).  Returns false
 // (the same in every thread of the CTA) when a TMA wait ran out: the window is then not used,
@@ -385,6 +431,8 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
   auto w_at = [&](int v, int t, int c) -> double & { return W[((size_t)v * T + t) * NW + c + G]; };
 
   // A: load the window of prim (and gamma) along each line
+  bool tame_ok = true;  // exact mode: whether every window value is tame (aph_math.cuh)
+  (void)tame_ok;
   if (a.tmaps && constg) {
     // one tensor copy of the T lines' whole extent into the staging area, then the window
     // cells -G..n+G-1 into W (the staging layout is [v][t][i] along x, [v][w][t] along y, z)
@@ -458,44 +506,25 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
 #endif
       }
       W[((size_t)v * T + t) * NW + w] = x;
+#if APH_EXACT
+      tame_ok = tame_ok && tame(x);
+#endif
     }
   }
+#if APH_EXACT
+  // every window value tame: the reconstruction takes the integer-pipe forms (same bits)
+  const bool tame_item = __syncthreads_and(tame_ok) != 0;
+#else
   __syncthreads();
+#endif
   // B-D: reconstruction; left state of face c+1 -> SL[c+1], right state of face c -> SR[c+1]
   if (RECON == RECON_PPM) {
-    const int w4 = n + 4, w3 = n + 3;
-    for (int it = tid; it < V * nl * w4; it += nth) {  // cells -2..n+1
-      const int v = it / (nl * w4);
-      const int r = it - v * nl * w4;
-      const int t = r / w4, c = r - t * w4 - 2;
-      const double qm = w_at(v, t, c - 1), q0 = w_at(v, t, c), qp = w_at(v, t, c + 1);
-      D2[((size_t)v * T + t) * w4 + c + 2] = ppm_d2(qm, q0, qp);
-      DD[((size_t)v * T + t) * w4 + c + 2] = ppm_dd(qm, q0, qp);
-    }
-    __syncthreads();
-    for (int it = tid; it < V * nl * w3; it += nth) {  // faces -1..n+1
-      const int v = it / (nl * w3);
-      const int r = it - v * nl * w3;
-      const int t = r / w3, f = r - t * w3 - 1;
-      const size_t o = ((size_t)v * T + t) * w4;
-      DPH[((size_t)v * T + t) * w3 + f + 1] =
-          ppm_face(w_at(v, t, f - 1), w_at(v, t, f), DD[o + f + 1], DD[o + f + 2], D2[o + f + 1],
-                   D2[o + f + 2]);
-    }
-    __syncthreads();
-    const int w2 = n + 2;
-    for (int it = tid; it < V * nl * w2; it += nth) {  // cells -1..n
-      const int v = it / (nl * w2);
-      const int r = it - v * nl * w2;
-      const int t = r / w2, c = r - t * w2 - 1;
-      const size_t o4 = ((size_t)v * T + t) * w4, o3 = ((size_t)v * T + t) * w3;
-      double ql, qr;
-      ppm_cell(w_at(v, t, c - 2), w_at(v, t, c - 1), w_at(v, t, c), w_at(v, t, c + 1),
-               w_at(v, t, c + 2), D2[o4 + c + 1], D2[o4 + c + 2], D2[o4 + c + 3], DPH[o3 + c + 1],
-               DPH[o3 + c + 2], ql, qr);
-      SL[((size_t)v * T + t) * w2 + c + 1] = ql;
-      SR[((size_t)v * T + t) * w2 + c + 1] = qr;
-    }
+#if APH_EXACT
+    if (tame_item)
+      ppm_window<true>(W, D2, DD, DPH, SL, SR, V, nl, T, n, G);
+    else
+#endif
+      ppm_window<false>(W, D2, DD, DPH, SL, SR, V, nl, T, n, G);
   } else {
     const int w2 = n + 2;
     for (int it = tid; it < V * nl * w2; it += nth) {
@@ -529,8 +558,12 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
       wr[IDN] = SR[IDN * vs + oR]; wr[IV1] = SR[ivx * vs + oR]; wr[IV2] = SR[ivy * vs + oR];
       wr[IV3] = SR[ivz * vs + oR]; wr[IPR] = SR[IPR * vs + oR];
 #if APH_EXACT
-      riemann<RS, false>(wl, wr, SL[nv * vs + oL], SL[(nv + 1) * vs + oL], SR[nv * vs + oR],
-                         SR[(nv + 1) * vs + oR], gc, flx);
+      if (tame_item)
+        riemann<RS, false, true>(wl, wr, SL[nv * vs + oL], SL[(nv + 1) * vs + oL], SR[nv * vs + oR],
+                                 SR[(nv + 1) * vs + oR], gc, flx);
+      else
+        riemann<RS, false, false>(wl, wr, SL[nv * vs + oL], SL[(nv + 1) * vs + oL], SR[nv * vs + oR],
+                                  SR[(nv + 1) * vs + oR], gc, flx);
 #else
       if (constg) {
         riemann<RS, true>(wl, wr, 0.0, 0.0, 0.0, 0.0, gc, flx);
@@ -581,8 +614,9 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
       }
     } else {
       const double vol = B.dx[0] * B.dx[1] * B.dx[2];
-#if !APH_EXACT
       const double ivol = 1.0 / vol;
+#if APH_EXACT
+      const bool vol_p2 = pow2_normal(vol);  // power-of-two volume: exact multiplication
 #endif
       const double beta_dt = a.beta * dt_of(a, B);
       unsigned long long mymin = ~0ULL;
@@ -599,7 +633,7 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
           double du = (area * F[of + 1] - area * F[of]);
           if (!first_pass) du = B.du[v * B.nint + icell] + du;
 #if APH_EXACT
-          const double div = -du / vol;
+          const double div = div_vol(-du, vol, ivol, vol_p2);
 #else
           const double div = -du * ivol;
 #endif
@@ -611,7 +645,7 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
           double du = (area * F[of + 1] - area * F[of]);
           if (!first_pass) du = B.du[v * B.nint + icell] + du;
 #if APH_EXACT
-          const double div = -du / vol;
+          const double div = div_vol(-du, vol, ivol, vol_p2);
 #else
           const double div = -du * ivol;
 #endif
@@ -702,15 +736,17 @@ __device__ void amr_update(const StageArgs &a, const Sched &sched, unsigned int 
     const long long nc = B.ncell;
     const long long ic = (long long)(j - p.ng) * B.nx[0] + (i - p.ng);
     const double vol = B.dx[0] * B.dx[1] * B.dx[2];
+    const double ivol = 1.0 / vol;
+    const bool vol_p2 = pow2_normal(vol);  // power-of-two volume: exact multiplication
     double u[NHYDRO];
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) {
-      const double div = -B.du[v * B.nint + ic] / vol;
+      const double div = div_vol(-B.du[v * B.nint + ic], vol, ivol, vol_p2);
       u[v] = a.gam0 * B.u0[v * nc + c] + a.gam1 * B.u1[v * nc + c] + beta_dt * div;
     }
     bool bad = false;
     for (int v = NHYDRO; v < p.nvar; ++v) {  // passive scalars
-      const double div = -B.du[v * B.nint + ic] / vol;
+      const double div = div_vol(-B.du[v * B.nint + ic], vol, ivol, vol_p2);
       const double x = a.gam0 * B.u0[v * nc + c] + a.gam1 * B.u1[v * nc + c] + beta_dt * div;
       B.u0[v * nc + c] = x;
       bad |= ((__double_as_longlong(x) >> 52) & 0x7ff) == 0x7ff;
@@ -757,9 +793,9 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
   unsigned long long dtmin = ~0ULL;
   unsigned int *ctr = a.ctl->work;
 
-  // phase 0: ghost zones
-  for (int it = sched.first(ctr + 0, a.ncell_items); it < a.ncell_items;
-       it = sched.next(ctr + 0, a.ncell_items, it)) {
+  // phase 0: ghost zones (unless the caller filled them, e.g. by a halo exchange)
+  for (int it = a.ghosts_given ? a.ncell_items : sched.first(ctr + 0, a.ncell_items);
+       it < a.ncell_items; it = sched.next(ctr + 0, a.ncell_items, it)) {
     const int2 w = a.cell_items[it];
     const StepBlock &B = a.blocks[w.x];
     if (!active_of(a, B)) continue;

@@ -51,8 +51,9 @@ __global__ void k_dt_initial(StepCtl *c, double cfl) {
   c->min_bits = ~0ULL;
 }
 
-// End of a step: advance time, dt_{n+1} = min(2 dt_n, cfl * min), clipped at tlim.
-__global__ void k_dt_policy(StepCtl *c, double cfl) {
+// End of a step: advance time, dt_{n+1} = min(2 dt_n, cfl * min), clipped at tlim.  given >= 0:
+// the estimate cfl * min comes from the caller (sharded packs: the minimum over all ranks).
+__global__ void k_dt_policy(StepCtl *c, double cfl, double given = -1.0) {
   const double used = c->dt;
   if (used > 0.0) {
     c->time += used;
@@ -62,7 +63,7 @@ __global__ void k_dt_policy(StepCtl *c, double cfl) {
   if (c->dt_fixed > 0.0) {
     next = c->time < c->tlim ? c->dt_fixed : 0.0;
   } else {
-    const double est = min_to_dt(c->min_bits, cfl);
+    const double est = given >= 0.0 ? given : min_to_dt(c->min_bits, cfl);
     const double two = 2.0 * used;
     next = (est < two) ? est : two;
     if (c->time < c->tlim && (c->tlim - c->time) < next) next = c->tlim - c->time;
@@ -1260,6 +1261,51 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
   if (best) aph_stepper_get_config(s, best);
   if (best_ms) *best_ms = best_t;
   return st;
+}
+
+aph_status aph_stepper_stage(aph_stepper s, int stage, int flags, void *stream) {
+  clear_error();
+  if (!s) return fail(APH_ERR_INVALID, "NULL stepper");
+  const std::vector<Stage> stages = stages_of(s->integrator);
+  if (stage < 0 || stage >= (int)stages.size())
+    return fail(APH_ERR_INVALID, "stage %d not in 0..%d", stage, (int)stages.size() - 1);
+  if (flags & ~APH_STAGE_GHOSTS_GIVEN) return fail(APH_ERR_INVALID, "unknown flags 0x%x", flags);
+  if ((flags & APH_STAGE_GHOSTS_GIVEN) && (s->d_members || s->dev.amr))
+    return fail(APH_ERR_UNSUPPORTED, "caller-filled ghost cells need a uniform block grid");
+  const bool last = stage + 1 == (int)stages.size();
+  const int recon = (s->integrator == APH_INTEGRATOR_VL2 && stage == 0) ? APH_RECON_DC : s->params.recon;
+  StageArgs a = stage_args(s, stage, stages[stage], last, false);
+  a.ghosts_given = (flags & APH_STAGE_GHOSTS_GIVEN) ? 1 : 0;
+  const cudaError_t e = launch_one(s, a, recon, (cudaStream_t)stream);
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "stepper stage");
+}
+
+aph_status aph_stepper_local_dt(aph_stepper s, double *estimate, void *stream) {
+  clear_error();
+  if (!s || !estimate) return fail(APH_ERR_INVALID, "NULL argument");
+  if (s->d_members) return fail(APH_ERR_UNSUPPORTED, "ensembles keep a dt per member");
+  StepCtl c;
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaMemcpy(&c, s->d_ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "stepper local dt");
+  if (c.error) return fail(c.error, "a stage's grid barrier gave up");
+  const double m = c.min_bits == ~0ULL ? DBL_MAX : [&] {
+    double x;
+    std::memcpy(&x, &c.min_bits, sizeof(x));
+    return x;
+  }();
+  *estimate = s->dev.cfl * m;
+  return APH_OK;
+}
+
+aph_status aph_stepper_end_step(aph_stepper s, double estimate, void *stream) {
+  clear_error();
+  if (!s) return fail(APH_ERR_INVALID, "NULL stepper");
+  if (s->d_members) return fail(APH_ERR_UNSUPPORTED, "ensembles keep a dt per member");
+  if (!(estimate > 0.0)) return fail(APH_ERR_INVALID, "the dt estimate must be positive");
+  k_dt_policy<<<1, 1, 0, (cudaStream_t)stream>>>(s->d_ctl, s->dev.cfl, estimate);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? APH_OK : cuda_fail(e, "stepper end step");
 }
 
 aph_status aph_diag_barrier_timeout(double timeout_s, void *stream) {

@@ -49,9 +49,15 @@ class MeshData:
     Fields are torch tensors ``(nblocks, nvar, nk, nj, ni)``: ``cons``, ``prim``, ``u1``,
     ``flux[d]`` and ``gamma`` (2 components).  ``pack`` is the C-ABI handle over all
     blocks; ``block_packs`` (on demand) hold one handle per meshblock.
+
+    face_fluxes: flux[d] shaped as Parthenon's face-centred arrays, one face longer along
+    d (``(nblocks, nvar, nk, nj, ni + 1)`` along x1), passed to the library with their
+    strides.  eos_lambda: also allocate the reference's ``eos_lambda`` field (3 components,
+    zero-initialised), which ConsToPrim touches as the reference's does.
     """
 
-    def __init__(self, cfg: MeshConfig, exact=False, device="cuda"):
+    def __init__(self, cfg: MeshConfig, exact=False, device="cuda", face_fluxes=False,
+                 eos_lambda=False):
         require_cuda()
         _capi.load()
         self.cfg = cfg
@@ -62,7 +68,17 @@ class MeshData:
         self.prim = torch.zeros(shape, **kw)
         self.u1 = torch.zeros(shape, **kw)
         self.gamma = torch.zeros(shape[:1] + (2,) + shape[2:], **kw)
-        self.flux = [torch.zeros(shape, **kw) if d < cfg.ndim else None for d in range(3)]
+        self.flux = []
+        for d in range(3):
+            if d >= cfg.ndim:
+                self.flux.append(None)
+                continue
+            fshape = list(shape)
+            if face_fluxes:
+                fshape[4 - d] += 1  # one more face along d
+            self.flux.append(torch.zeros(fshape, **kw))
+        self.eos_lambda = (torch.zeros(shape[:1] + (3,) + shape[2:], **kw) if eos_lambda
+                           else None)
         self.params = make_params(cfg, exact, cfg.nvar)
         self.pack = self._make_pack(range(cfg.nblocks))
         nb = (ctypes.c_int * 3)(*cfg.blocks_per_dim)
@@ -78,9 +94,14 @@ class MeshData:
         blk.gamma = self.gamma[b].data_ptr()
         blk.u1 = self.u1[b].data_ptr()
         for d in range(3):
-            blk.flux[d] = self.flux[d][b].data_ptr() if self.flux[d] is not None else None
+            f = self.flux[d]
+            blk.flux[d] = f[b].data_ptr() if f is not None else None
+            if f is not None and tuple(f.shape) != tuple(self.cons.shape):
+                blk.flux_stride[d][:] = [f.stride(1), f.stride(2), f.stride(3)]
             blk.nx[d] = cfg.block_nx[d]
             blk.dx[d] = cfg.dx[d]
+        if self.eos_lambda is not None:
+            blk.eos_lambda = self.eos_lambda[b].data_ptr()
         return blk
 
     def _make_pack(self, blocks):

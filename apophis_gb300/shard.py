@@ -1,7 +1,13 @@
 """Sharding a uniform block grid over ranks (one GPU per rank): block partition, halo
-exchange of the ghost zones between ranks, and the dt min-reduction -- the exchange steps of
-the reference's MPI driver (apophis_driver.cpp:68-104 boundary communication, and the
-global dt min of EstimateTimestep).
+exchange of the ghost zones between ranks, the dt min-reduction, and the sharded RK step that
+strings them together -- the exchange steps of the reference's MPI driver
+(apophis_driver.cpp:68-104 boundary communication, and the global dt min of EstimateTimestep).
+
+``step(engine)`` runs one RK step of a rank's shard: every stage exchanges the halo and
+advances the shard's blocks, then the ranks' dt estimates are reduced to their minimum and
+the dt policy applied.  ``GpuShard`` is the engine of the CUDA path: the batched stepper over
+the rank's blocks, driven stage by stage with the ghost cells the exchange filled
+(aph_stepper_stage with APH_STAGE_GHOSTS_GIVEN, aph_stepper_local_dt, aph_stepper_end_step).
 
 The partition gives each rank a contiguous range of blocks in Z (Morton) order.  The exchange
 is planned from global metadata only (every rank derives the same plan): every ghost cell of
@@ -11,6 +17,8 @@ one message per peer, and scattered into the ghost cells (with the reflecting si
 Data stay on the ranks' devices; torch.distributed moves them (NCCL between GPUs, gloo on
 CPU), with no host round trip on the GPU path.
 """
+import dataclasses
+import ctypes
 from dataclasses import dataclass
 from typing import Dict, List
 
@@ -70,6 +78,17 @@ class HaloPlan:
     # per peer: flat destination indices of the received values, and their sign (+1 / -1)
     recv: Dict[int, np.ndarray]
     recv_sign: Dict[int, np.ndarray]
+    _dev: Dict = dataclasses.field(default_factory=dict, repr=False)
+
+    def on(self, device, dtype):
+        """The plan's index and sign arrays as tensors on device, made once per device."""
+        key = (str(device), dtype)
+        if key not in self._dev:
+            self._dev[key] = (
+                {q: torch.as_tensor(v, device=device) for q, v in self.send.items()},
+                {q: torch.as_tensor(v, device=device) for q, v in self.recv.items()},
+                {q: torch.as_tensor(v, dtype=dtype, device=device) for q, v in self.recv_sign.items()})
+        return self._dev[key]
 
 
 def plan_halo(cfg: MeshConfig, parts: List[List[int]], rank: int, nvar: int = None) -> HaloPlan:
@@ -137,8 +156,8 @@ def exchange(local: torch.Tensor, plan: HaloPlan, group=None):
     peer (point-to-point, all posted before any wait)."""
     flat = local.view(-1)
     dev = local.device
-    idx = {q: torch.as_tensor(v, device=dev) for q, v in plan.send.items()}
-    bufs = {q: flat.index_select(0, i) for q, i in idx.items()}
+    send_idx, recv_idx, recv_sign = plan.on(dev, local.dtype)
+    bufs = {q: flat.index_select(0, i) for q, i in send_idx.items()}
     me = plan.rank
     incoming = {q: torch.empty(len(v), dtype=local.dtype, device=dev) for q, v in plan.recv.items()
                 if q != me}
@@ -150,17 +169,91 @@ def exchange(local: torch.Tensor, plan: HaloPlan, group=None):
         ops.append(dist.P2POp(dist.irecv, buf, q, group))
     reqs = dist.batch_isend_irecv(ops) if ops else []
     if me in plan.recv:  # sources on this rank
-        vals = bufs[me] * torch.as_tensor(plan.recv_sign[me], dtype=local.dtype, device=dev)
-        flat.index_copy_(0, torch.as_tensor(plan.recv[me], device=dev), vals)
+        flat.index_copy_(0, recv_idx[me], bufs[me] * recv_sign[me])
     for r in reqs:
         r.wait()
     for q, buf in incoming.items():
-        vals = buf * torch.as_tensor(plan.recv_sign[q], dtype=local.dtype, device=dev)
-        flat.index_copy_(0, torch.as_tensor(plan.recv[q], device=dev), vals)
+        flat.index_copy_(0, recv_idx[q], buf * recv_sign[q])
 
 
 def global_dt(local_dt: float, group=None, device="cpu") -> float:
-    """The step's dt: the minimum of every rank's estimate (an allreduce-min)."""
+    """The step's dt: the minimum of every rank's estimate (an allreduce-min; the estimate
+    itself without a process group)."""
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(local_dt)
     t = torch.tensor([local_dt], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MIN, group=group)
     return float(t.item())
+
+
+def step(engine, nsteps=1, group=None):
+    """nsteps sharded RK steps of one rank's engine.  The engine provides ``nstages``,
+    ``stage(i)`` (exchange the halo, then advance stage i of the step), ``local_estimate()``
+    (cfl * min over its interior cells of the new state) and ``end_step(estimate)`` (the dt
+    policy with the estimate of all ranks); ``device`` is where the dt reduction runs."""
+    for _ in range(nsteps):
+        for i in range(engine.nstages):
+            engine.stage(i)
+        est = global_dt(engine.local_estimate(), group, engine.device)
+        engine.end_step(est)
+
+
+@dataclass
+class _ShardConfig:
+    """A rank's blocks as a pack of their own: nlocal blocks in a row, with the mesh's dx."""
+    base: MeshConfig
+    nlocal: int
+
+    def mesh(self) -> MeshConfig:
+        b = self.base
+        bn = b.block_nx
+        # the cell widths of the blocks are passed explicitly (the mesh's, bit for bit); the
+        # boundaries of the local pack never act (the exchange fills every ghost cell)
+        return dataclasses.replace(b, mesh_nx=(bn[0] * self.nlocal, bn[1], bn[2]),
+                                   bc=(("periodic", "periodic"),) * 3)
+
+
+class GpuShard:
+    """A rank's blocks on its GPU, stepped by the batched stepper stage by stage, with the
+    ghost cells filled by the halo exchange before each stage."""
+
+    def __init__(self, cfg: MeshConfig, parts: List[List[int]], rank: int, cons_local,
+                 exact=False, tlim=None, group=None):
+        from . import _capi
+        from .hydro import STAGES, stream_handle
+        from .stepper import Stepper
+        self._capi, self._stream = _capi, stream_handle
+        self.cfg = cfg
+        self.plan = plan_halo(cfg, parts, rank)
+        self.group = group
+        local_cfg = _ShardConfig(cfg, len(parts[rank])).mesh()
+        self.st = Stepper(local_cfg, cons_local, exact=exact, tlim=tlim, dx=cfg.dx)
+        # the stepper's dt_0 is this rank's estimate: reduce it over the ranks
+        self.device = self.st.cons.device
+        s = self.st.status()
+        dt0 = global_dt(s["dt"], group, self.device)
+        _capi.call("aph_stepper_set_clock", self.st.h, s["time"], dt0, s["ncycle"], stream_handle())
+        self.nstages = len(STAGES[cfg.integrator])
+
+    @property
+    def cons(self):
+        return self.st.cons
+
+    def stage(self, i):
+        exchange(self.st.cons, self.plan, self.group)
+        self._capi.call("aph_stepper_stage", self.st.h, i, self._capi.APH_STAGE_GHOSTS_GIVEN,
+                        self._stream())
+
+    def local_estimate(self):
+        out = ctypes.c_double()
+        self._capi.call("aph_stepper_local_dt", self.st.h, ctypes.byref(out), self._stream())
+        return out.value
+
+    def end_step(self, estimate):
+        self._capi.call("aph_stepper_end_step", self.st.h, float(estimate), self._stream())
+
+    def status(self):
+        return self.st.status()
+
+    def close(self):
+        self.st.close()

@@ -23,7 +23,7 @@ TUNE_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "a
 
 class Stepper:
     def __init__(self, cfg: MeshConfig, cons0=None, exact=False, tlim=None, fixed_dt=0.0,
-                 cons=None):
+                 cons=None, dx=None):
         require_cuda()
         _capi.load()
         self.cfg = cfg
@@ -33,11 +33,12 @@ class Stepper:
             cons.copy_(torch.as_tensor(np.ascontiguousarray(cons0)))
         self.cons = cons
         blocks = (_capi.aph_block * cfg.nblocks)()
+        dx = cfg.dx if dx is None else dx  # explicit widths: a rank's share of a larger mesh
         for b in range(cfg.nblocks):
             blocks[b].cons = self.cons[b].data_ptr()
             for d in range(3):
                 blocks[b].nx[d] = cfg.block_nx[d]
-                blocks[b].dx[d] = cfg.dx[d]
+                blocks[b].dx[d] = dx[d]
         self._blocks = blocks
         desc = _capi.aph_stepper_desc()
         desc.params = make_params(cfg, exact, cfg.nvar)

@@ -5,6 +5,12 @@ Headline workload (the reference benchmark configuration that fits one GPU): 3D 
 CFL 0.3, gamma 5/3, FP64, synthetic initial data.  A "step" is one full RK2 step of the
 whole pack (2 stages + the CFL dt reduction).
 
+Arithmetic mode (--mode): exact (the default) computes the reference's FP64 operations in the
+reference's order with one rounding each and is bit-identical to the oracle, so it carries
+the parity claim; fast (fused multiply-adds, shared reciprocals, constant adiabatic indices)
+is timed beside it as other_mode and is not parity-carrying (the reference's PPM limiter
+switches branches on its one-ulp differences).
+
 value   zone-updates/s of the batched path (one persistent launch per stage over all 64
         meshblocks, the step replayed as a CUDA graph), state resident in HBM.
 e2e     the same through the C ABI with the state in pinned host memory as the packed
@@ -57,14 +63,41 @@ UNIT = "zone-updates/s"
 WORKLOAD = ("kh3d 256^3: 64 meshblocks of 64^3, 4 ghost cells, PPM+HLLC, RK2, CFL 0.3, "
             "gamma 5/3, FP64")
 BYTES_PER_ZONE_UPDATE = 200.0   # RK2 with 5 FP64 conserved variables
-# FP64 work of the stage kernel (fast mode) per RK2 zone-update: DADD + DMUL + DFMA thread
-# instructions the kernel executes, from the ncu capture in profiles/stage_kernel_kh3d.md
-# (1,020 in the stage with the dt epilogue + 961 in the other, per zone)
-FP64_LANE_OPS_PER_ZONE_UPDATE = 1981.0
-FP64_LANES_PER_CLK_PER_SM = 2.0    # DFMA lanes per clock per SM on GB300 (profiles/fp64_pipe_gb300.md)
-# DRAM bytes (read + write) per zone per stage launch, same capture (128^3 pack of 64^3 blocks;
-# the 256^3 launches process the same blocks, 8x as many)
-TRAFFIC_BYTES_PER_ZONE_LAUNCH = 628.3
+# FP64 work of the stage kernel per RK2 zone-update on this workload: the DADD + DMUL + DFMA
+# thread instructions the kernel executes (ncu sass counters of one stage launch of each kind
+# on a 128^3 pack of 64^3 blocks, per zone), by arithmetic mode
+FP64_LANE_OPS_PER_ZONE_UPDATE = {"fast": 1981.0, "exact": None}
+FP64_LANES_PER_CLK_PER_SM = 2.0    # DFMA lanes per clock per SM on GB300 (measured)
+# DRAM bytes (read + write) per zone per stage launch, same captures (the 256^3 launches
+# process 8x the blocks of the 128^3 capture, so traffic is scaled by zones)
+TRAFFIC_BYTES_PER_ZONE_LAUNCH = {"fast": 628.3, "exact": None}
+TRAFFIC_LAUNCH = {"fast": "8 lines, dynamic schedule (not the tuned launch)", "exact": None}
+PARITY = {
+    "exact": "bit-identical to the oracle (the reference's FP64 CPU path): one step of this "
+             "256^3 pack with this launch, 50 steps of 128^3, the refined RT pack over 100 "
+             "steps and blast members to t = 0.1 (tests/test_gpu_headline.py)",
+    "fast": "not parity-carrying: PPM limiter branches switch on one-ulp differences (50 of "
+            "16.7M cells off by up to 8e-7 after one step of this pack; end-of-run L1(rho) "
+            "< 1e-10 on KH, 1.5e-4 on blast members)",
+}
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return None
+
+
+def workload_config(cfg, ws):
+    """The config object of the JSON line (the same in both arms)."""
+    return {"workload": WORKLOAD, "zones": cfg.zones(), "meshblocks": cfg.nblocks,
+            "parallelism": "replica per rank" if ws > 1 else "none (one pack)",
+            "l2": "no flush: inputs larger than L2 (state 1.0 GB, ~4 GB working set)"}
 
 
 def peaks():
@@ -175,7 +208,7 @@ def amr_leg(args, warmup):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / n
 
-    st = amr.AmrStepper(cfg, cons, exact=False)
+    st = amr.AmrStepper(cfg, cons, exact=args.exact)
     tune = None if args.no_tune else st.autotune(trial_steps=2)
     st.step(warmup)
     st.status()
@@ -184,20 +217,21 @@ def amr_leg(args, warmup):
     bms = timed(st.step, nsteps)
     status = st.status()
     st.close()
-    out = {"workload": "rt2d_amr: 1440 meshblocks (160 of 32^2 at level 0, 256 + 1024 of 16^2 "
+    out = {"mode": "exact" if args.exact else "fast",
+           "workload": "rt2d_amr: 1440 meshblocks (160 of 32^2 at level 0, 256 + 1024 of 16^2 "
                        "at levels 1-2), 491,520 zones, PPM+HLLC, RK2, gravity -0.1, FP64",
            "batched": {"value": zones / (bms * 1e-3), "ms_per_step": bms, "steps": nsteps,
                        "stage_ms": stage_ms, "launches_per_step": 3,
                        "launch": tune["config"] if tune else None, "sim_time": status["time"]}}
     if not args.no_plain:
-        drv = amr.AmrDriver(cfg, cons, exact=False)
+        drv = amr.AmrDriver(cfg, cons, exact=args.exact)
         drv.run(nsteps=2)
         pms = timed(lambda n: drv.run(nsteps=n), 20)
         out["plain_per_pack"] = {"value": zones / (pms * 1e-3), "ms_per_step": pms}
         drv.md.close()
         del drv
         # per meshblock, host-driven: each kernel launched once per block through the C ABI
-        drv = amr.AmrDriver(cfg, cons, exact=False, per_block=True)
+        drv = amr.AmrDriver(cfg, cons, exact=args.exact, per_block=True)
         drv.run(nsteps=1)
         hms = timed(lambda n: drv.run(nsteps=n), 2)
         # the same launches replayed from one CUDA graph (no host cost): fixed dt, each block's
@@ -243,7 +277,7 @@ def ensemble_leg(args):
     import torch
     from apophis_gb300 import ensemble
     ens, flat = ensemble.blast_ensemble()
-    st = ensemble.EnsembleStepper(ens, flat, exact=False)
+    st = ensemble.EnsembleStepper(ens, flat, exact=args.exact)
     tune = None if args.no_tune else st.autotune(trial_steps=2)
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     a, b = ev(), ev()
@@ -256,7 +290,8 @@ def ensemble_leg(args):
     ms = st.member_status()
     st.close()
     zu = sum(c.zones() * k for c, k in zip(ens.members, ms["ncycle"]))
-    return {"workload": "64 blast2d members (%d blocks of 64^2, %d zones), PPM+HLLC, RK2, "
+    return {"mode": "exact" if args.exact else "fast",
+            "workload": "64 blast2d members (%d blocks of 64^2, %d zones), PPM+HLLC, RK2, "
                         "CFL 0.3, to t = 0.1" % (ens.nblocks, ens.zones()),
             "value": zu / sec, "unit": UNIT, "seconds": sec, "zone_updates": zu,
             "member_steps_min_max": [min(ms["ncycle"]), max(ms["ncycle"])],
@@ -405,11 +440,11 @@ def table_leg(args):
         out["cpu_cores"] = O.num_threads()
         for label, per_block, n in (("gpu_plain_per_meshblock", True, max(1, nsteps // 2)),
                                     ("gpu_plain_per_pack", False, nsteps)):
-            d = hydro.Driver(cfg, cons, exact=False, per_block=per_block)
+            d = hydro.Driver(cfg, cons, exact=args.exact, per_block=per_block)
             d.run(nsteps=1, fixed_dt=fixed_dt)
             out[label] = zones / gpu_time(lambda k: d.run(nsteps=k, fixed_dt=fixed_dt), n)
             d.md.close()
-        st = Stepper(cfg, cons, exact=False, fixed_dt=fixed_dt)
+        st = Stepper(cfg, cons, exact=args.exact, fixed_dt=fixed_dt)
         st.autotune(trial_steps=1)
         st.step(3)
         st.status()
@@ -435,7 +470,7 @@ def table_leg(args):
         t = time.perf_counter()
         m.run(nsteps=1)
         t_cpu += time.perf_counter() - t
-        d = hydro.Driver(mcfg, mcons, exact=False)
+        d = hydro.Driver(mcfg, mcons, exact=args.exact)
         d.run(nsteps=1)
         t_pack += gpu_time(lambda k: d.run(nsteps=k), 2)
         d.md.close()
@@ -455,12 +490,51 @@ def run_reference(args, cfg, cons):
     line = {"impl": "reference", "metric": METRIC, "value": zps, "unit": UNIT, "n_gpus": ws,
             "steps": nsteps, "warmup": args.warmup, "ms_per_step": el / nsteps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "parallelism": "host threads"},
+            "data": "synthetic", "config": workload_config(cfg, ws),
             "cpu_baseline": {"value": zps, "unit": UNIT, "cores": cores, "kind": "port",
+                             "cpu_model": cpu_model(),
                              "sample": "%d full RK2 steps of the 256^3 pack after %d warm-up steps"
                                        % (nsteps, args.warmup)},
             "e2e": {"value": zps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def timed_stepper(cfg, cons, exact, args, dist, local):
+    """Autotune (or set) the launch, warm up, and time args.steps graph-replayed steps with
+    CUDA events on the launching stream; returns (stepper, ms per step, stage ms, clocks,
+    launch)."""
+    import torch
+    from apophis_gb300.stepper import Stepper
+    st = Stepper(cfg, cons, exact=exact)
+    if args.launch:
+        c = st.config
+        c.update(json.loads(args.launch))
+        st.set_config(c)
+    elif not args.no_tune:
+        st.autotune(trial_steps=1)
+    stream = torch.cuda.current_stream()
+    st.step(args.warmup)
+    st.status()
+    stage_ms = st.profile(nsteps=2)  # per-stage kernel durations (roofline time)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        st.step(args.steps)
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return st, ms, stage_ms, clk.summary(), st.config
 
 
 def main():
@@ -470,12 +544,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--n", type=int, default=256, help="mesh cells per side")
+    ap.add_argument("--mode", default="exact", choices=["exact", "fast"],
+                    help="arithmetic mode of the headline (exact: bit-identical to the oracle)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--launch", default=None,
                     help="JSON launch configuration of the stepper (keys of aph_stepper_config); "
                          "used instead of the autotuner, e.g. for reproducible profiles")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-meshblock path")
+    ap.add_argument("--no-fast", action="store_true", help="skip the other arithmetic mode's leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-amr", action="store_true", help="skip the refined-pack leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint ratio leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the blast-ensemble leg")
@@ -483,11 +561,13 @@ def main():
                     help="run one extra leg alone and print its object (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    exact = args.mode == "exact"
     if args.only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         from apophis_gb300 import _build
         _build.build()
+        args.exact = exact
         out = {"amr": lambda: amr_leg(args, args.warmup), "ensemble": lambda: ensemble_leg(args),
                "adjoint": adjoint_leg, "table": lambda: table_leg(args)}[args.only]()
         print(json.dumps({"only": args.only, args.only: out}), flush=True)
@@ -504,114 +584,105 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     from apophis_gb300 import _build, hydro
-    from apophis_gb300.stepper import Stepper
     _build.build()
 
     zones = cfg.zones()
-    st = Stepper(cfg, cons, exact=False)
-    tune = None
-    if args.launch:
-        c = st.config
-        c.update(json.loads(args.launch))
-        st.set_config(c)
-        tune = {"config": st.config}
-    elif not args.no_tune:
-        tune = st.autotune(trial_steps=1)
-    stream = torch.cuda.current_stream()
-    st.step(args.warmup)
-    st.status()
-    # per-stage kernel durations (roofline numerator time)
-    stage_ms = st.profile(nsteps=2)
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        barrier()
-        e0.record(stream)
-        st.step(args.steps)
-        e1.record(stream)
-        barrier()
-    ms = e0.elapsed_time(e1) / args.steps
+    st, ms, stage_ms, clocks, launch = timed_stepper(cfg, cons, exact, args, dist, local)
     status = st.status()
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     value = zones * ws / (ms * 1e-3)
     launches_per_step = 3  # two stage kernels + the dt-policy kernel
 
     # e2e: the state in pinned host memory as the packed interiors, through the C ABI
     # (aph_stepper_load_interiors / _store_interiors): every step loads its input from the
     # host and stores its result back, inside the timed region
-    host = torch.empty(st.interior_shape(), dtype=torch.float64, pin_memory=True)
-    st.store_interiors(host)
-    nbytes = host.numel() * 8
-
-    def e2e_step():
-        st.load_interiors(host)
-        st.step(1)
+    e2e = None
+    if not args.no_e2e:
+        stream = torch.cuda.current_stream()
+        host = torch.empty(st.interior_shape(), dtype=torch.float64, pin_memory=True)
         st.store_interiors(host)
+        nbytes = host.numel() * 8
 
-    for _ in range(max(1, min(args.warmup, 2))):  # first transfers of a fresh pinned buffer
-        e2e_step()
-    with ClockSampler(local) as clk_e2e:
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
+        def e2e_step():
+            st.load_interiors(host)
+            st.step(1)
+            st.store_interiors(host)
+
+        def barrier():
+            if dist is not None:
+                dist.barrier()
+            torch.cuda.synchronize()
+
+        for _ in range(max(1, min(args.warmup, 2))):  # first transfers of a fresh pinned buffer
             e2e_step()
-        barrier()
-        t1 = time.perf_counter()  # before the sampler stops (its shutdown is not the step's)
-    e2e_ms = (t1 - t0) * 1e3 / args.steps
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = zones * ws / (e2e_ms * 1e-3)
-    # the host link's share of an e2e step: the load and the store alone (CUDA events)
-    link = {}
-    for name, fn in (("load", lambda: st.load_interiors(host)), ("store", lambda: st.store_interiors(host))):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(3):
-            fn()
-        b.record(stream)
-        torch.cuda.synchronize()
-        t = a.elapsed_time(b) / 3
-        link[name + "_ms"] = t
-        link[name + "_gbs"] = nbytes / (t * 1e-3) / 1e9
+        with ClockSampler(local) as clk_e2e:
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                e2e_step()
+            barrier()
+            t1 = time.perf_counter()  # before the sampler stops (its shutdown is not the step's)
+        e2e_ms = (t1 - t0) * 1e3 / args.steps
+        if dist is not None:
+            t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        # the host link's share of an e2e step: the load and the store alone (CUDA events)
+        link = {}
+        for name, fn in (("load", lambda: st.load_interiors(host)),
+                         ("store", lambda: st.store_interiors(host))):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(3):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            t = a.elapsed_time(b) / 3
+            link[name + "_ms"] = t
+            link[name + "_gbs"] = nbytes / (t * 1e-3) / 1e9
+        e2e = {"value": zones * ws / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "mode": args.mode,
+               "host_link": link, "clocks": clk_e2e.summary()}
+        del host
     st.close()
     del st
     torch.cuda.empty_cache()
 
+    # the other arithmetic mode, same workload and timing
+    other = None
+    if not args.no_fast:
+        omode = "fast" if exact else "exact"
+        ost, oms, ostage, oclk, olaunch = timed_stepper(cfg, cons, not exact, args, dist, local)
+        ost.close()
+        del ost
+        torch.cuda.empty_cache()
+        other = {"mode": omode, "value": zones * ws / (oms * 1e-3), "ms_per_step": oms,
+                 "stage_ms": ostage, "launch": olaunch, "clocks": oclk, "parity": PARITY[omode]}
+
     # plain per-meshblock launch path, bounded sample
     plain = None
     if rank == 0 and not args.no_plain:
-        drv = hydro.Driver(cfg, cons, exact=False, per_block=True)
+        drv = hydro.Driver(cfg, cons, exact=exact, per_block=True)
         drv.run(nsteps=1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         drv.run(nsteps=2)
         torch.cuda.synchronize()
         pms = (time.perf_counter() - t0) * 1e3 / 2
-        plain = {"value": zones / (pms * 1e-3), "ms_per_step": pms,
+        plain = {"value": zones / (pms * 1e-3), "ms_per_step": pms, "mode": args.mode,
                  "launches_per_step": 2 * cfg.nblocks * (1 + 3 + 1) + 2 + 2 + cfg.nblocks,
                  "driver": "one launch per kernel per meshblock"}
         del drv
         torch.cuda.empty_cache()
         # reference-style granularity: one launch per kernel per pack (the Kokkos kernels over a
         # MeshBlockPack)
-        drv = hydro.Driver(cfg, cons, exact=False, per_block=False)
+        drv = hydro.Driver(cfg, cons, exact=exact, per_block=False)
         drv.run(nsteps=1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         drv.run(nsteps=2)
         torch.cuda.synchronize()
         kms = (time.perf_counter() - t0) * 1e3 / 2
-        plain_pack = {"value": zones / (kms * 1e-3), "ms_per_step": kms,
+        plain_pack = {"value": zones / (kms * 1e-3), "ms_per_step": kms, "mode": args.mode,
                       "launches_per_step": 2 * (1 + 3 + 1) + 2 + 2 + 1,
                       "driver": "one launch per kernel per pack"}
         del drv
@@ -621,41 +692,44 @@ def main():
     stage_sum = sum(stage_ms)
     per_launch_bytes = BYTES_PER_ZONE_UPDATE * zones / len(stage_ms)
     achieved = per_launch_bytes / (stage_sum / len(stage_ms) * 1e-3) / 1e9
-    clocks = clk.summary()
     sm_mhz = clocks.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
     fp64_peak = FP64_LANES_PER_CLK_PER_SM * 152 * sm_mhz * 1e6 / 1e9  # G lane-ops/s
+    traffic = TRAFFIC_BYTES_PER_ZONE_LAUNCH[args.mode]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "zones": zones, "meshblocks": cfg.nblocks,
-                   "parallelism": "replica per GPU" if ws > 1 else "1 GPU",
-                   "l2": "no flush: inputs larger than L2 (state 1.0 GB, ~4 GB working set)",
-                   "launch": tune["config"] if tune else None},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "host_link": link,
-                "clocks": clk_e2e.summary()},
+        "config": workload_config(cfg, ws),
+        "mode": args.mode, "parity": PARITY[args.mode], "launch": launch,
+        "e2e": e2e,
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm,
-                     "traffic": TRAFFIC_BYTES_PER_ZONE_LAUNCH * zones,
-                     "traffic_note": "ncu DRAM bytes per zone of a 128^3 capture x zones",
-                     "kernel": "k_stage (batched stage)", "stage_ms": stage_ms,
-                     "peak_source": peak_kind},
-        "fp64_pipe": {"note": "the FP64 pipe binds this kernel (ncu: 79 % busy, DRAM 3 %); achieved counts the DADD/DMUL/DFMA it executes",
+                     "traffic": traffic * zones / len(stage_ms) if traffic else None,
+                     "traffic_note": ("ncu DRAM bytes per zone of one stage launch on a 128^3 "
+                                      "pack (%s) x zones" % TRAFFIC_LAUNCH[args.mode])
+                                     if traffic else "no capture of this mode's launch",
+                     "kernel": "k_stage (batched stage, %s mode)" % args.mode,
+                     "stage_ms": stage_ms, "peak_source": peak_kind},
+        "fp64_pipe": {"note": "the FP64 pipe binds this kernel; achieved counts the DADD/DMUL/DFMA "
+                              "it executes (ncu)",
                       "peak_source": "2 DFMA lanes/clk/SM x 152 SMs x sampled SM clock"},
         "clocks": clocks,
         "time_check": {"sim_time": status["time"], "ncycle": status["ncycle"]},
     }
-    if FP64_LANE_OPS_PER_ZONE_UPDATE:
-        ach = FP64_LANE_OPS_PER_ZONE_UPDATE * zones / (stage_sum * 1e-3) / 1e9
+    ops = FP64_LANE_OPS_PER_ZONE_UPDATE[args.mode]
+    if ops:
+        ach = ops * zones / (stage_sum * 1e-3) / 1e9
         line["fp64_pipe"].update({"achieved": ach, "peak": fp64_peak, "unit": "G lane-ops/s",
-                                  "frac": ach / fp64_peak})
+                                  "frac": ach / fp64_peak, "ops_per_zone_update": ops})
+    if other is not None:
+        line["other_mode"] = other
     if plain is not None:
         line["plain"] = plain
         line["plain_per_pack"] = plain_pack
         line["batched_vs_plain"] = value / ws / plain["value"]
         line["batched_vs_plain_per_pack"] = value / ws / plain_pack["value"]
+    args.exact = exact
     if rank == 0 and not args.no_amr:
         line["amr"] = amr_leg(args, args.warmup)
         line["gpu_launches_amr_batched_step"] = 3
@@ -666,10 +740,11 @@ def main():
         if not args.no_ensemble:
             line["ensemble_adjoint"] = ensemble_adjoint_leg()
     if rank == 0 and not args.no_cpu:
-        runs = [cpu_baseline(cfg, cons, 1) for _ in range(3)]
-        zps, cores, el = sorted(runs)[1]
+        runs = [cpu_baseline(cfg, cons, 1) for _ in range(5)]
+        zps, cores, el = sorted(runs)[2]
         line["cpu_baseline"] = {"value": zps, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": "median of 3 runs of 1 full RK2 step of the 256^3 pack, "
+                                "cpu_model": cpu_model(),
+                                "sample": "median of 5 runs of 1 full RK2 step of the 256^3 pack, "
                                           "each after 1 warm-up step (%.1f s per run)" % el}
         if "amr" in line:
             line["amr"]["cpu_baseline"] = cpu_baseline_amr()

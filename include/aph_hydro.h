@@ -57,6 +57,17 @@ typedef struct aph_block {
                       flux[d] at (n,k,j,i) is the face on the low side of cell (k,j,i) */
   int nx[3];       /* interior cells per dimension (1 for an unused dimension) */
   double dx[3];    /* cell widths; for an unused dimension the mesh extent along it */
+  long long flux_stride[3][3]; /* strides in doubles of flux[d] over (n, k, j), i being
+                      contiguous; all three 0: the shape of cons.  A flux array of its own
+                      shape, e.g. Parthenon's face-centred (nvar, nk, nj, ni + 1) along x1,
+                      passes its strides (element (n, k, j, i) at n*s[0] + k*s[1] + j*s[2] + i,
+                      face i on the low side of cell i); each row must hold the faces of the
+                      cons row (plus one along d), each plane its rows, each component its
+                      planes */
+  double *eos_lambda; /* "eos_lambda" (hydro.cpp:241-249), 3 components, the shape of cons;
+                      may be NULL.  Only ConsToPrim touches it, as the reference's does for
+                      the ideal gas: lT (component 2) becomes 7 where it is 0
+                      (hydro.cpp:491-493) */
 } aph_block;
 
 /* Hydro package parameters (InitializeHydro, src/hydro/hydro.cpp:33-349). */
@@ -105,9 +116,9 @@ aph_status aph_pack_create(const aph_hydro_params *params, const aph_block *bloc
  * physical boundaries bc[2*d + side] (side 0 inner, 1 outer); needed by
  * aph_hydro_fill_ghosts. */
 aph_status aph_pack_set_topology(aph_pack pack, const int nb[3], const int bc[6]);
-/* Blocks form a statically refined 2D mesh (ndim 2, nvar 5): ghost fill uses the face
- * tables (copy, 2x2 restriction, minmod-linear prolongation) and the flux-divergence update
- * corrects coarse cells at coarse-fine faces to the mean of the fine face fluxes (the
+/* Blocks form a statically refined 2D mesh (ndim 2; passive scalars allowed): ghost fill uses
+ * the face tables (copy, 2x2 restriction, minmod-linear prolongation) and the flux-divergence
+ * update corrects coarse cells at coarse-fine faces to the mean of the fine face fluxes (the
  * flux-correction tasks of apophis_driver.cpp:68, 74-76). bc as in aph_pack_set_topology. */
 aph_status aph_pack_set_amr(aph_pack pack, const aph_amr_block *amr, const int bc[6]);
 /* Host-only check of a refined mesh's face tables against the blocks' interior sizes
@@ -268,6 +279,20 @@ aph_status aph_stepper_history(aph_stepper stepper, double out[2], void *stream)
  * step or run). */
 aph_status aph_stepper_load_interiors(aph_stepper stepper, const double *src, void *stream);
 aph_status aph_stepper_store_interiors(aph_stepper stepper, double *dst, void *stream);
+/* Sharded packs (one rank's blocks of a larger uniform grid; the reference's MPI driver,
+ * apophis_driver.cpp:68-104, exchanges their ghost zones and reduces dt across ranks):
+ * a step driven stage by stage.  aph_stepper_stage enqueues stage `stage` (0-based) of the
+ * current step with the stepper's dt; with APH_STAGE_GHOSTS_GIVEN the caller has filled every
+ * ghost cell of the state (a halo exchange) and the stage's own ghost fill is skipped (uniform
+ * block grids only).  After the last stage, aph_stepper_local_dt returns (blocking) this
+ * pack's estimate cfl * min over its interior cells of the new state, and
+ * aph_stepper_end_step applies the dt policy (time += dt; dt = min(2 dt, estimate), clipped at
+ * tlim) with the caller's estimate, the minimum over all ranks.  Stage by stage without the
+ * flag and with this pack's own estimate is exactly aph_stepper_step. */
+#define APH_STAGE_GHOSTS_GIVEN 1
+aph_status aph_stepper_stage(aph_stepper stepper, int stage, int flags, void *stream);
+aph_status aph_stepper_local_dt(aph_stepper stepper, double *estimate, void *stream);
+aph_status aph_stepper_end_step(aph_stepper stepper, double estimate, void *stream);
 aph_status aph_stepper_get_config(aph_stepper stepper, aph_stepper_config *cfg);
 aph_status aph_stepper_set_config(aph_stepper stepper, const aph_stepper_config *cfg);
 /* Advance nsteps steps without the graph, timing each stage launch with CUDA events on
@@ -284,6 +309,13 @@ aph_status aph_stepper_autotune(aph_stepper stepper, int trial_steps, aph_steppe
  * runs out; the context stays usable.  Stepper status calls also return APH_ERR_STATE once an
  * update has produced a NaN or an infinity. */
 aph_status aph_diag_barrier_timeout(double timeout_s, void *stream);
+
+/* Test probe (no counterpart in the reference): evaluates on the device, for the n device
+ * values x, the integer-pipe operations the exact arithmetic mode uses on tame operands
+ * (op 0: x / 6.0 by the exact remainder, 1: 0.5 * x, 2: 2.0 * x as exponent steps, 3: 1.0 if
+ * x is tame, else 0.0) into out, so that tests can compare them bit for bit with the IEEE
+ * operations they stand for.  Asynchronous on stream. */
+aph_status aph_diag_exact_ops(int op, const double *x, double *out, long long n, void *stream);
 
 /* ---- adjoint of the step --------------------------------------------------------------
  * Hand-written reverse mode of the full fixed-dt step: ConsToPrim, the PPM, PLM or
@@ -308,7 +340,9 @@ aph_status aph_adjoint_step(aph_adjoint adjoint, const double *u_n, double dt, d
 aph_status aph_adjoint_step_vjp(aph_adjoint adjoint, const double *u_n, double dt,
                                 const double *lam_next, double *lam_n, void *stream);
 /* Rollout of nsteps steps with the fixed dt schedule dts[] (host array) from u0, keeping a
- * checkpoint every checkpoint_every steps on the device; writes the final state. */
+ * checkpoint every checkpoint_every steps on the device; writes the final state.  Also sizes
+ * the reverse sweep's segment storage (checkpoint_every steps of stage-input primitives),
+ * so that aph_adjoint_backward allocates nothing. */
 aph_status aph_adjoint_forward(aph_adjoint adjoint, const double *u0, int nsteps, const double *dts,
                                int checkpoint_every, double *u_final, void *stream);
 /* The same with a dt per member and step: dts[k * nmembers + m] (one member without an

@@ -83,6 +83,23 @@ def test_pack_create_rejects_bad_blocks():
     assert st == 1
 
 
+def test_pack_create_rejects_flux_strides_too_small():
+    """Caller-given flux layouts must hold each component's face array (a row of ni + 1
+    faces along x1, nj + 1 rows along x2, planes of those rows)."""
+    lib = _capi.load()
+    h = ctypes.c_void_p()
+    ni, nj = 8 + 6, 8 + 6  # nx + 2 nghost
+    for d, strides in [(0, [ni * nj, ni * nj, ni]),            # x1 rows without the extra face
+                       (1, [ni * nj, ni * nj, ni]),            # x2 planes without the extra row
+                       (0, [1, (ni + 1) * nj, ni + 1])]:       # components overlapping
+        b = _block()
+        b.flux_stride[d][:] = strides
+        st = lib.aph_pack_create(ctypes.byref(_params()), (_capi.aph_block * 1)(b), 1,
+                                 ctypes.byref(h))
+        assert st == 1 and "strides" in lib.aph_last_error().decode(), (d, strides)
+        assert not h.value
+
+
 def test_null_pack_calls_fail_cleanly():
     lib = _capi.load()
     assert lib.aph_hydro_cons_to_prim(None, None) == 1

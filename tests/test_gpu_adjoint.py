@@ -184,12 +184,32 @@ def test_one_step_gradient_matches_finite_differences(cuda):
     assert errs.max() < 1e-6, errs
 
 
+def _taped_grad_checkpointed(cfg, W0, dts, tgt):
+    """The taped restatement's gradient of a long rollout, one torch checkpoint per step (the
+    graph of one step is rebuilt during the backward pass, so 200 steps of 512^2 fit)."""
+    from torch.utils.checkpoint import checkpoint
+    rho0 = W0[0].clone().requires_grad_(True)
+    vy0 = W0[2].clone().requires_grad_(True)
+    W = W0.clone()
+    W[0] = rho0
+    W[2] = vy0
+    U = TR.prim_to_cons(W, cfg.gm1)
+    for dt in dts:
+        U = checkpoint(TR.step, U, dt, cfg.dx, cfg.gamma, cfg.recon, cfg.rsolver, cfg.integrator,
+                       cfg.ndim, use_reentrant=False)
+    loss = torch.sqrt(torch.sum((U[0] - tgt) ** 2))
+    return torch.autograd.grad(loss, (rho0, vy0))
+
+
 @pytest.mark.slow
 def test_differentiable_kh_config_fd(cuda):
     """Differentiable KH 2D 512^2 (64 meshblocks of 64^2), PLM + HLLE, RK2, 200 steps with a
-    checkpoint every 20, 32 seeded directions, central differences with step 1e-6.  The
-    exact gradient of the scheme agrees with these differences only to ~1e-3 (the limiter's
-    kinks, see the module docstring); the adjoint must do as well as that."""
+    checkpoint every 20, 32 seeded directions, central differences with step 1e-6.
+
+    The adjoint's gradient equals the taped restatement's (torch.autograd through the same
+    200 steps) to 1e-9, and on every direction the two directional derivatives agree to
+    1e-9: the differences' disagreement with the gradient (median ~1e-3) is the same for
+    both, so it belongs to the scheme's kinks (module docstring), not to the adjoint."""
     cfg, _ = kh_setup(512, 64, "hlle", "rk2")
     adj = Adjoint(cfg)
     W0, Wt, dts, gen = _setup_rollout(cfg, 200, seed=5)
@@ -198,9 +218,89 @@ def test_differentiable_kh_config_fd(cuda):
     rho0 = W0[0].clone().requires_grad_(True)
     vy0 = W0[2].clone().requires_grad_(True)
     _, gr, gv = _loss_and_grad(cfg, adj, rho0, vy0, W0, dts, 20, tgt)
-    errs = _fd_rel(cfg, adj, W0, dts, 20, tgt, gr, gv, 1e-6, 32, gen)
-    print("config-4 FD relative errors: median %.2e max %.2e" % (np.median(errs), errs.max()))
+    tr, tv = _taped_grad_checkpointed(cfg, W0, dts, tgt)
+    err = torch.sqrt(((gr - tr) ** 2).sum() + ((gv - tv) ** 2).sum()) / torch.sqrt((tr ** 2).sum() + (tv ** 2).sum())
+    assert float(err) < 1e-9, float(err)
+    errs, errs_taped = [], []
+    h = 1e-6
+    for _ in range(32):
+        dr = torch.randn(gr.shape, dtype=torch.float64, device="cuda", generator=gen)
+        dv = torch.randn(gv.shape, dtype=torch.float64, device="cuda", generator=gen)
+        with torch.no_grad():
+            lp = _loss_and_grad(cfg, adj, W0[0] + h * dr, W0[2] + h * dv, W0, dts, 20, tgt, False)
+            lm = _loss_and_grad(cfg, adj, W0[0] - h * dr, W0[2] - h * dv, W0, dts, 20, tgt, False)
+        fd = (lp - lm) / (2 * h)
+        an = float((gr * dr).sum() + (gv * dv).sum())
+        at = float((tr * dr).sum() + (tv * dv).sum())
+        assert abs(an - at) <= 1e-9 * abs(at), (an, at)
+        errs.append(abs(fd - an) / max(abs(fd), abs(an)))
+        errs_taped.append(abs(fd - at) / max(abs(fd), abs(at)))
+    errs, errs_taped = np.array(errs), np.array(errs_taped)
+    print("differentiable KH config, FD relative errors: adjoint median %.2e max %.2e; taped "
+          "median %.2e max %.2e" % (np.median(errs), errs.max(), np.median(errs_taped),
+                                     errs_taped.max()))
+    assert np.allclose(errs, errs_taped, rtol=1e-4, atol=1e-12)
     assert np.median(errs) < 1e-2 and errs.max() < 5e-2, errs
+
+
+def _branches(cfg, W, dts):
+    """The branch record of the taped restatement's rollout from primitive state W."""
+    TR.BRANCHES = []
+    try:
+        with torch.no_grad():
+            U = TR.prim_to_cons(W, cfg.gm1)
+            for dt in dts:
+                U = TR.step(U, dt, cfg.dx, cfg.gamma, cfg.recon, cfg.rsolver, cfg.integrator, cfg.ndim)
+        return TR.BRANCHES
+    finally:
+        TR.BRANCHES = None
+
+
+def test_ppm_hllc_gradient_matches_fd_where_no_branch_switches(cuda):
+    """PPM + HLLC (2D KH, one 16^2 meshblock, 2 RK2 steps): on seeded directions whose
+    central-difference pair u +- h d takes the same branch in every limiter and wave-speed
+    decision of the rollout (the branch record of the taped restatement at both points), the
+    adjoint's directional derivative agrees with the differences to 1e-6 relative.  The base
+    state carries small cell-to-cell noise so that no decision is an exact tie (a smooth KH
+    band is constant along x, and its zero second differences tie in PPM's min and sign
+    tests); across a switched branch PPM's limiters jump and differences do not converge."""
+    cfg, _ = kh_setup(16, 16, "hllc", "rk2", "ppm")
+    adj = Adjoint(cfg)
+    nsteps = 2
+    W0, Wt, dts, _ = _setup_rollout(cfg, nsteps, seed=17)
+    gen = torch.Generator().manual_seed(18)  # host generator: the same draws on every GPU
+    noise = torch.randn(tuple(W0.shape), dtype=torch.float64, generator=gen) * 1e-3
+    noise[3] = 0.0  # v_z stays exactly zero in 2D
+    W0 = W0 + noise.cuda() * W0.abs().amax(dim=(1, 2, 3), keepdim=True)
+    with torch.no_grad():
+        tgt = global_from_pack(cfg, adj.forward(pack_from_global(cfg, TR.prim_to_cons(Wt, cfg.gm1)), dts, 1))[0]
+    rho0 = W0[0].clone().requires_grad_(True)
+    vy0 = W0[2].clone().requires_grad_(True)
+    _, gr, gv = _loss_and_grad(cfg, adj, rho0, vy0, W0, dts, 1, tgt)
+    h = 1e-8
+    checked, errs = 0, []
+    for _ in range(32):
+        dr = torch.randn(tuple(gr.shape), dtype=torch.float64, generator=gen).cuda()
+        dv = torch.randn(tuple(gv.shape), dtype=torch.float64, generator=gen).cuda()
+        Wp, Wm = W0.clone(), W0.clone()
+        Wp[0] += h * dr
+        Wp[2] += h * dv
+        Wm[0] -= h * dr
+        Wm[2] -= h * dv
+        bp, bm = _branches(cfg, Wp, dts), _branches(cfg, Wm, dts)
+        if not all(torch.equal(a, b) for a, b in zip(bp, bm)):
+            continue  # a branch switches between the two points
+        with torch.no_grad():
+            lp = _loss_and_grad(cfg, adj, Wp[0], Wp[2], W0, dts, 1, tgt, False)
+            lm = _loss_and_grad(cfg, adj, Wm[0], Wm[2], W0, dts, 1, tgt, False)
+        fd = (lp - lm) / (2 * h)
+        an = float((gr * dr).sum() + (gv * dv).sum())
+        errs.append(abs(fd - an) / max(abs(fd), abs(an)))
+        checked += 1
+    print("PPM+HLLC: %d of 32 directions without a switched branch; FD errors %s" % (
+        checked, np.array2string(np.array(errs), precision=2)))
+    assert checked >= 4
+    assert max(errs) < 1e-6, errs
 
 
 def test_checkpoint_spacing_does_not_change_gradient(cuda):

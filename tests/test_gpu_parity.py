@@ -123,3 +123,52 @@ def test_sod_full_run_l1(cuda):
     rho_o = m.get("cons")[0, 0, 0, 0, g:-g]
     l1 = np.mean(np.abs(rho_g - rho_o))
     assert l1 < 1e-10, l1
+
+
+@pytest.mark.parametrize("wl", [w for w in WORKLOADS if w[0] in ("sod_plm_hlle", "kh2d_ppm_hllc",
+                                                                    "kh3d_ppm_hllc")],
+                         ids=lambda w: w[0])
+def test_face_centred_flux_arrays_and_eos_lambda(cuda, wl):
+    """Parthenon's own field layout: flux arrays one face longer along their direction
+    (passed with their strides) and the eos_lambda field.  ConsToPrim, CalculateFluxes and
+    the update must give the oracle's bits (exact mode), the face arrays must hold the
+    oracle's fluxes at every interior face, and eos_lambda's lT must become 7 as the
+    reference's ConsToPrim makes it (hydro.cpp:491-493)."""
+    name, cfg, cons = wl
+    m = _oracle_ready(cfg, cons)
+    cons_g, prim_ref, gamma_ref = m.get("cons"), m.get("prim"), m.get("gamma")
+    md = hydro.MeshData(cfg, exact=True, face_fluxes=True, eos_lambda=True)
+    for d in range(cfg.ndim):
+        assert md.flux[d].shape[4 - d] == md.cons.shape[4 - d] + 1
+    md.set_cons(cons_g)
+    hydro.ConsToPrim(md)
+    hydro.CalculateFluxes(md)
+    torch.cuda.synchronize()
+    assert_parity(md.prim.cpu().numpy(), prim_ref, True, what="prim")
+    lam = md.eos_lambda.cpu().numpy()
+    assert (lam[:, 2] == 7.0).all() and (lam[:, :2] == 0.0).all()
+    nb = cfg.nblocks
+    ref_flux = []
+    for b in range(nb):
+        fl = [np.zeros_like(cons_g[b]) for _ in range(3)]
+        O.calculate_fluxes(np.ascontiguousarray(prim_ref[b]), np.ascontiguousarray(gamma_ref[b]),
+                           fl, cfg.block_nx, cfg.ng, cfg.ndim, cfg.recon, cfg.rsolver)
+        ref_flux.append(fl)
+    nk, nj, ni = md.cons.shape[2:]
+    for d in range(cfg.ndim):
+        got = md.flux[d].cpu().numpy()[:, :, :nk, :nj, :ni]  # same (k, j, i) face indexing
+        sl = (slice(None), slice(None)) + interior_faces(cfg, d)
+        ref = np.stack([ref_flux[b][d] for b in range(nb)])[sl]
+        assert_parity(got[sl], ref, True, what="flux%d" % (d + 1))
+    u1 = cons_g.copy()
+    md.u1.copy_(torch.from_numpy(u1))
+    hydro.UpdateWithFluxDivergence(md, 0.5, 0.5, 1.3e-3)
+    torch.cuda.synchronize()
+    ref = cons_g.copy()
+    for b in range(nb):
+        O.update(ref[b], np.ascontiguousarray(u1[b]), ref_flux[b], cfg.block_nx, cfg.ng, cfg.ndim,
+                 cfg.dx, 0.5, 0.5, 1.3e-3)
+    sk, sj, si = cfg.interior
+    sl = (slice(None), slice(None), sk, sj, si)
+    assert_parity(md.cons.cpu().numpy()[sl], ref[sl], True, what="update")
+    md.close()

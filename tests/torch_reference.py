@@ -10,6 +10,16 @@ import torch
 
 C2 = 2.99792458e10 ** 2
 TINY = 1.0e-20
+
+# Branch record: while BRANCHES is a list, every limiter and wave-speed decision (the boolean
+# masks of the piecewise definitions) is appended to it, so that two evaluations can be checked
+# for taking the same branches everywhere (no kink between them).
+BRANCHES = None
+
+
+def _rec(*masks):
+    if BRANCHES is not None:
+        BRANCHES.extend(m.detach().clone() for m in masks)
 STAGES = {
     "rk1": [(0.0, 1.0, 1.0)],
     "rk2": [(0.0, 1.0, 1.0), (0.5, 0.5, 0.5)],
@@ -56,6 +66,7 @@ def _ppm(q, axis, G):
     qd_mag_is_qa = qa.abs() < m
     qd = torch.where(qd_mag_is_qa, qa, torch.where(sa, -m, m))
     qd = torch.where(match, qd, torch.zeros_like(qd))
+    _rec(sa, d2m1 < 0, d20 < 0, d20.abs() < d2m1.abs(), qd_mag_is_qa, qa_tmp * qb_tmp < 0)
     dph = torch.where(qa_tmp * qb_tmp < 0, avg - qd / 6.0, dph)
     nc = n + 2                                # cells -1..n
     lo, hi = dph.narrow(axis, 0, nc), dph.narrow(axis, 1, nc)
@@ -78,6 +89,10 @@ def _ppm(q, axis, G):
     ql_e = torch.where(app, qi + rho * dqp, hi)
     qr_m = torch.where(dqm.abs() >= 2.0 * dqp.abs(), qi - 2.0 * dqp, lo)
     ql_m = torch.where(dqp.abs() >= 2.0 * dqm.abs(), qi + 2.0 * dqm, hi)
+    _rec(dqm * dqp > 0, (qip1 - qi) * (qi - qim1) > 0, sd, e2m1 < 0, e20 < 0, e2p1 < 0,
+         e20.abs() < e2m1.abs(), e2p1.abs() < torch.minimum(e2m1.abs(), e20.abs()),
+         d2qf.abs() < mm, big, app, dqm < 0, dqp < 0, dqm.abs() >= 2.0 * dqp.abs(),
+         dqp.abs() >= 2.0 * dqm.abs())
     ql = torch.where(ext, ql_e, ql_m)
     qr = torch.where(ext, qr_e, qr_m)
     return ql.narrow(axis, 0, n + 1), qr.narrow(axis, 1, n + 1)
@@ -97,6 +112,7 @@ def _recon(q, recon, axis, G=2):
     dqr = qp - q0
     dq2 = dql * dqr
     pos = dq2 > 0
+    _rec(pos)
     den = torch.where(pos, dql + dqr, torch.ones_like(dql))
     dqm = torch.where(pos, dq2 / den, torch.zeros_like(dql))
     qlp = q0 + dqm  # left state of face c+1, c = -1..n
@@ -125,6 +141,7 @@ def hlle(wl, wr, gamma):
     qr = torch.where(pmid > pr, 1.0 + k * (pmid / pr - 1.0), torch.ones_like(pr))
     al = ul - cl * ql
     ar = ur + cr * qr
+    _rec(pmid > pl, pmid > pr, ar > 0, al < 0)
     bp = torch.where(ar > 0, ar, torch.zeros_like(ar))
     bm = torch.where(al < 0, al, torch.zeros_like(al))
     vxl, vxr = ul - bm, ur - bp
@@ -163,6 +180,7 @@ def hllc(wl, wr, gamma):
     mr = -(rr * vxr)
     sstar = (tl - tr) / (ml + mr)
     cp = (ml * tr + mr * tl) / (ml + mr)
+    _rec(bl, br, sr > 0, sl < 0, cp > 0, sstar >= 0)
     cp = torch.where(cp > 0, cp, torch.zeros_like(cp))
     wxl, wxr = ul - bm, ur - bp
     fl = [rl * wxl, rl * ul * wxl + pl, rl * vl * wxl, rl * zl * wxl, el * wxl + pl * ul]
