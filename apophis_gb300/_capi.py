@@ -138,6 +138,8 @@ SIGNATURES = {
     "aph_stepper_end_step": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p], ctypes.c_int),
     "aph_diag_exact_ops": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
                             ctypes.c_void_p], ctypes.c_int),
+    "aph_diag_exact_ops2": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                             ctypes.c_longlong, ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_member_status": ([ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int),
                                    ctypes.c_void_p], ctypes.c_int),
     "aph_stepper_get_config": ([ctypes.c_void_p, ctypes.POINTER(aph_stepper_config)],

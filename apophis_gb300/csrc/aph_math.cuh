@@ -123,6 +123,88 @@ __device__ __forceinline__ double div6_x(double x) {
   return ((b << 1) != 0 && mag(r1) < mag(r0)) ? q1 : q0;
 }
 
+// ---- IEEE double additions and small multiplications on the integer pipe ---------------
+// Round-to-nearest-even sums and products by 3, 5/4 and 6 computed with 64-bit integer
+// arithmetic (the textbook alignment with a sticky bit, guard bits, renormalisation and
+// rounding), for operands that are zero or normal with 2^-900 < |x| < 2^900 and results that
+// stay so -- every value the reconstruction forms from a tame window.  They return exactly the
+// bits of the FP64 instruction they replace, on a pipe that retires ~60 times more lanes per
+// clock than GB300's FP64 pipe.
+
+// Pack a positive significand S (leading 1 at bit 62, sticky bits below bit 10) with biased
+// exponent e and sign bit sg, rounding to nearest even.
+__device__ __forceinline__ double round_pack_x(unsigned long long sg, long long e, unsigned long long S) {
+  const unsigned long long r = S & 0x3ffULL;
+  unsigned long long m = S >> 10;  // 53 bits, leading 1 at bit 52
+  if (r > 0x200ULL || (r == 0x200ULL && (m & 1ULL))) ++m;
+  if (m >> 53) {  // rounding carried into bit 53
+    m >>= 1;
+    ++e;
+  }
+  return __longlong_as_double((long long)(sg | ((unsigned long long)e << 52) | (m & 0xfffffffffffffULL)));
+}
+
+// RN(a + b)
+__device__ __forceinline__ double add_x(double a, double b) {
+  unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+  unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+  unsigned long long ma = ua & 0x7fffffffffffffffULL, mb = ub & 0x7fffffffffffffffULL;
+  if (mb > ma) {  // |a| >= |b| from here on
+    const unsigned long long t = ua;
+    ua = ub;
+    ub = t;
+    const unsigned long long tm = ma;
+    ma = mb;
+    mb = tm;
+  }
+  const unsigned long long sg = ua & 0x8000000000000000ULL;
+  if (mb == 0) {  // b is a zero: a, or the sum of two zeros (-0 only for -0 + -0)
+    if (ma != 0) return __longlong_as_double((long long)ua);
+    return __longlong_as_double((long long)(ua & ub));
+  }
+  const long long ea = (long long)(ma >> 52), eb = (long long)(mb >> 52);
+  const long long d = ea - eb;
+  if (d > 55) return __longlong_as_double((long long)ua);  // |b| below a quarter ulp of a
+  // significands with 9 guard bits (leading 1 at bit 61); b's shifted out bits as a sticky bit
+  const unsigned long long A = ((ma & 0xfffffffffffffULL) | 0x10000000000000ULL) << 9;
+  const unsigned long long Bf = ((mb & 0xfffffffffffffULL) | 0x10000000000000ULL) << 9;
+  const unsigned long long Bt = Bf >> d;
+  const unsigned long long st = ((Bf << (63 - d)) << 1) != 0 ? 1ULL : 0ULL;  // only for d >= 10
+  long long e = ea;
+  unsigned long long S;
+  if (((ua ^ ub) >> 63) == 0) {  // same signs: the sum's floor, sticky; leading 1 at bit 61 or 62
+    S = (A + Bt) | st;
+    if (S >> 62) {
+      S = (S >> 1) | (S & 1ULL);
+      ++e;
+    }
+    S <<= 1;  // leading 1 at bit 62
+  } else {  // the difference's floor (sticky: b was truncated, subtract one more), then sticky
+    S = A - Bt - st;
+    if (S == 0) return 0.0;  // x - x = +0 (st is 0 then)
+    const int sh = __clzll((long long)S) - 1;  // bring the leading 1 to bit 62 (sh <= 2 if st)
+    S = (S << sh) | st;
+    e -= sh - 1;
+  }
+  return round_pack_x(sg, e, S);
+}
+__device__ __forceinline__ double sub_x(double a, double b) {
+  return add_x(a, __longlong_as_double(__double_as_longlong(b) ^ (long long)0x8000000000000000ULL));
+}
+
+// RN(k * x) for k = C * 2^S2 with a small odd integer C (3: k = 3 or 6; 5: k = 1.25)
+template <int C, int S2>
+__device__ __forceinline__ double mulk_x(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long m = u & 0x7fffffffffffffffULL;
+  if (m == 0) return x;  // k * +-0 = +-0
+  const unsigned long long P = ((m & 0xfffffffffffffULL) | 0x10000000000000ULL) * (unsigned long long)C;
+  const int sh = __clzll((long long)P) - 1;  // leading 1 to bit 62
+  // P << sh holds the value's significand in bits 62..10: exponent field E + 10 + S2 - sh
+  const long long e = (long long)(m >> 52) + 10 + S2 - sh;
+  return round_pack_x(u & 0x8000000000000000ULL, e, P << sh);
+}
+
 // ---- gamma-dependent constants of a pack (fast mode) ---------------------------
 struct GasConsts {
   double gm1, igm1, gamma;      // eos/gm1, 1/gm1, gm1+1
@@ -240,7 +322,7 @@ __device__ __forceinline__ void plm(double q_im1, double q_i, double q_ip1, doub
 template <bool TAME = false>
 __device__ __forceinline__ double ppm_dd(double qm1, double q0, double qp1) {
 #if APH_EXACT
-  if (TAME) return half_x(qp1 - q0) + half_x(q0 - qm1);
+  if (TAME) return add_x(half_x(sub_x(qp1, q0)), half_x(sub_x(q0, qm1)));
   return 0.5 * (qp1 - q0) + 0.5 * (q0 - qm1);
 #else
   return 0.5 * (qp1 - qm1);  // the same quantity with one rounding
@@ -248,7 +330,7 @@ __device__ __forceinline__ double ppm_dd(double qm1, double q0, double qp1) {
 }
 template <bool TAME = false>
 __device__ __forceinline__ double ppm_d2(double qm1, double q0, double qp1) {
-  if (APH_EXACT && TAME) return (qm1 + qp1) - twice_x(q0);
+  if (APH_EXACT && TAME) return sub_x(add_x(qm1, qp1), twice_x(q0));
   return (qm1 + qp1) - 2.0 * q0;
 }
 // Face between cells c-1 (value qm1) and c (value q0): ddm1 = dd(c-1), dd0 = dd(c),
@@ -258,20 +340,20 @@ __device__ __forceinline__ double ppm_face(double qm1, double q0, double ddm1, d
                                            double d2m1, double d20) {
 #if APH_EXACT
   if (TAME) {
-    const double s = qm1 + q0;
+    const double s = add_x(qm1, q0);  // the additions and the x3, x5/4 scalings on the integer pipe
     const double avg = half_x(s);
-    double dph = avg + div6_x(ddm1 - dd0);
-    const double qa = 3.0 * (s - twice_x(dph));
+    double dph = add_x(avg, div6_x(sub_x(ddm1, dd0)));
+    const double qa = mulk_x<3, 0>(sub_x(s, twice_x(dph)));
     double qd = 0.0;
     const bool sa = is_neg(qa);
     if (sa == is_neg(d2m1) && sa == is_neg(d20)) {
       const unsigned long long mb = mag(d2m1), mc = mag(d20);
-      const double m = PPM_C2 * from_bits(mc < mb ? mc : mb);
+      const double m = mulk_x<5, -2>(from_bits(mc < mb ? mc : mb));  // PPM_C2 = 5/4
       const unsigned long long mm = mag(m), ma = mag(qa);
       qd = flip_if(from_bits(ma < mm ? ma : mm), sa);
     }
     // (dph - qm1) * (q0 - dph) < 0, the differences being nonzero and their product normal
-    if (strictly_outside(dph, qm1, q0)) dph = avg - div6_x(qd);
+    if (strictly_outside(dph, qm1, q0)) dph = sub_x(avg, div6_x(qd));
     return dph;
   }
 #endif
@@ -312,10 +394,11 @@ __device__ __forceinline__ void ppm_cell(double q_im2, double q_im1, double q_i,
                                          double dph_lo, double dph_hi, double &ql_ip1,
                                          double &qr_i) {
   constexpr bool T = APH_EXACT && TAME;
-  const double d2qf = 6.0 * (dph_lo + dph_hi - (T ? twice_x(q_i) : 2.0 * q_i));
+  const double d2qf = T ? mulk_x<3, 1>(sub_x(add_x(dph_lo, dph_hi), twice_x(q_i)))
+                        : 6.0 * (dph_lo + dph_hi - 2.0 * q_i);
   double qr = dph_lo, ql = dph_hi;
-  const double dqf_minus = q_i - qr;
-  const double dqf_plus = ql - q_i;
+  const double dqf_minus = T ? sub_x(q_i, qr) : q_i - qr;
+  const double dqf_plus = T ? sub_x(ql, q_i) : ql - q_i;
 #if APH_EXACT
   bool extremum;
   if (T) {  // the two products' signs, as in ppm_face
@@ -337,7 +420,8 @@ __device__ __forceinline__ void ppm_cell(double q_im2, double q_im1, double q_i,
       const unsigned long long m0 = mag(d20), m1 = mag(d2p1);
       m = m0 < m ? m0 : m;
       m = m1 < m ? m1 : m;
-      const unsigned long long ms = mag(PPM_C2 * from_bits(m)), md = mag(d2qf);
+      const unsigned long long ms = mag(T ? mulk_x<5, -2>(from_bits(m)) : PPM_C2 * from_bits(m));
+      const unsigned long long md = mag(d2qf);
       qe = flip_if(from_bits(md < ms ? md : ms), sd);
     }
     unsigned long long mx = mag(q_im2);
@@ -350,16 +434,18 @@ __device__ __forceinline__ void ppm_cell(double q_im2, double q_im1, double q_i,
     if (mag(d2qf) > mag(1.0e-12 * from_bits(mx))) rho = qe / d2qf;
     if (le(rho, 1.0 - 1.0e-12)) {
 #if APH_EXACT
-      qr = q_i - rho * dqf_minus;
-      ql = q_i + rho * dqf_plus;
+      qr = T ? sub_x(q_i, rho * dqf_minus) : q_i - rho * dqf_minus;
+      ql = T ? add_x(q_i, rho * dqf_plus) : q_i + rho * dqf_plus;
 #else
       qr = fma(-rho, dqf_minus, q_i);
       ql = fma(rho, dqf_plus, q_i);
 #endif
     }
   } else {
-    if (mag(dqf_minus) >= twice_mag(dqf_plus)) qr = q_i - (T ? twice_x(dqf_plus) : 2.0 * dqf_plus);
-    if (mag(dqf_plus) >= twice_mag(dqf_minus)) ql = q_i + (T ? twice_x(dqf_minus) : 2.0 * dqf_minus);
+    if (mag(dqf_minus) >= twice_mag(dqf_plus))
+      qr = T ? sub_x(q_i, twice_x(dqf_plus)) : q_i - 2.0 * dqf_plus;
+    if (mag(dqf_plus) >= twice_mag(dqf_minus))
+      ql = T ? add_x(q_i, twice_x(dqf_minus)) : q_i + 2.0 * dqf_minus;
   }
   ql_ip1 = ql;
   qr_i = qr;

@@ -316,6 +316,11 @@ aph_status aph_diag_barrier_timeout(double timeout_s, void *stream);
  * x is tame, else 0.0) into out, so that tests can compare them bit for bit with the IEEE
  * operations they stand for.  Asynchronous on stream. */
 aph_status aph_diag_exact_ops(int op, const double *x, double *out, long long n, void *stream);
+/* The same for the integer-pipe IEEE additions and small multiplications: op 0: x + y,
+ * 1: x - y, 2: 3 * x, 3: 6 * x, 4: 1.25 * x (y unused by ops 2-4), for operands zero or normal
+ * with 2^-900 < |x| < 2^900. */
+aph_status aph_diag_exact_ops2(int op, const double *x, const double *y, double *out, long long n,
+                               void *stream);
 
 /* ---- adjoint of the step --------------------------------------------------------------
  * Hand-written reverse mode of the full fixed-dt step: ConsToPrim, the PPM, PLM or

@@ -5,7 +5,8 @@ div6_x (x / 6.0 by the exact remainder) is checked on random values over its who
 range and on values made to put x / 6 close to a representable number or to a midpoint
 between two (where a faithful but incorrectly rounded quotient would show); half_x and
 twice_x on the range reachable from tame windows, zeros of both signs included; tame on
-values at and around its thresholds.
+values at and around its thresholds; the integer-pipe IEEE additions (add_x, sub_x) and
+multiplications by 3, 6 and 5/4 (mulk_x) on their whole stated range.
 """
 import ctypes
 
@@ -79,3 +80,46 @@ def test_tame_thresholds(cuda):
                   np.nan, 1e-300, 1e300])
     want = np.where((x == 0) | ((np.abs(x) >= edges[0]) & (np.abs(x) < edges[1])), 1.0, 0.0)
     np.testing.assert_array_equal(_run(3, x), want)
+
+
+def _run2(op, x, y):
+    xd = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    yd = torch.from_numpy(np.ascontiguousarray(y)).cuda()
+    out = torch.empty_like(xd)
+    st = _capi.load().aph_diag_exact_ops2(op, ctypes.c_void_p(xd.data_ptr()),
+                                           ctypes.c_void_p(yd.data_ptr()),
+                                           ctypes.c_void_p(out.data_ptr()), xd.numel(),
+                                           hydro.stream_handle())
+    assert st == 0, _capi.load().aph_last_error()
+    return out.cpu().numpy()
+
+
+def test_integer_pipe_add_matches_ieee(cuda):
+    """add_x / sub_x against IEEE addition: random pairs with any exponent difference, near
+    cancellations (b close to -a within a few ulps), equal exponents, one operand far below
+    the other's ulp, and signed zeros."""
+    rng = np.random.Generator(np.random.PCG64(7))
+    n = 2_000_000
+    a = _random_in_range(rng, n, -800, 800)
+    kind = rng.integers(0, 5, n)
+    b = _random_in_range(rng, n, -800, 800)
+    near = -(a.view(np.int64) + rng.integers(-64, 65, n)).view(np.float64)
+    b = np.where(kind == 1, near, b)
+    close = (a.view(np.int64) ^ rng.integers(0, 1 << 50, n)).view(np.float64)
+    b = np.where(kind == 2, np.where(rng.random(n) < 0.5, close, -close), b)
+    far = a * 2.0 ** rng.integers(-70, 71, n).astype(np.float64) * (1 + rng.random(n))
+    b = np.where(kind == 3, np.where(rng.random(n) < 0.5, far, -far), b)
+    z = rng.random(n)
+    b = np.where(z < 0.01, 0.0, np.where(z < 0.02, -0.0, b))
+    a = np.where(rng.random(n) < 0.005, -0.0, a)
+    ok = np.isfinite(a + b) & ((np.abs(a + b) > 2.0 ** -900) | (a + b == 0))
+    a, b = a[ok], b[ok]
+    _bits_equal(_run2(0, a, b), a + b, "add_x")
+    _bits_equal(_run2(1, a, b), a - b, "sub_x")
+
+
+def test_integer_pipe_small_multiplies_match_ieee(cuda):
+    rng = np.random.Generator(np.random.PCG64(8))
+    x = np.concatenate([_random_in_range(rng, 2_000_000, -800, 800), np.array([0.0, -0.0, 1.0])])
+    for op, k in ((2, 3.0), (3, 6.0), (4, 1.25)):
+        _bits_equal(_run2(op, x, x), k * x, "x%g" % k)
