@@ -291,7 +291,7 @@ def _params(cfg, exact):
 class AmrMeshData:
     """Flat device fields of a refined pack and its C-ABI pack (plus per-block partitions)."""
 
-    def __init__(self, cfg: AmrConfig, exact=False):
+    def __init__(self, cfg: AmrConfig, exact=True):
         import torch
         from . import _capi
         from .hydro import require_cuda
@@ -358,7 +358,7 @@ class AmrDriver:
     """Per-kernel path on a refined pack: one launch per kernel per pack, or (per_block) one
     launch per kernel per meshblock; ghost fill and the flux correction are per pack."""
 
-    def __init__(self, cfg: AmrConfig, cons0, exact=False, per_block=False):
+    def __init__(self, cfg: AmrConfig, cons0, exact=True, per_block=False):
         import torch
         from . import hydro
         self.cfg = cfg
@@ -424,7 +424,7 @@ class AmrStepper(_StepperBase):
     """Batched path on a refined pack: one persistent launch per stage over all blocks (the
     same aph_stepper_* handle as the uniform stepper, created with a face table)."""
 
-    def __init__(self, cfg: AmrConfig, cons0, exact=False, tlim=None, fixed_dt=0.0):
+    def __init__(self, cfg: AmrConfig, cons0, exact=True, tlim=None, fixed_dt=0.0):
         import torch
         from . import _capi
         from .hydro import require_cuda

@@ -116,7 +116,7 @@ class EnsembleStepper(_StepperBase):
     def interior_values(self):
         return self.ens.nvar * sum(c.zones() for c in self.ens.members)
 
-    def __init__(self, ens: Ensemble, cons0, exact=False, fixed_dt=0.0):
+    def __init__(self, ens: Ensemble, cons0, exact=True, fixed_dt=0.0):
         import torch
         from . import _capi
         from .hydro import require_cuda

@@ -56,7 +56,7 @@ class MeshData:
     zero-initialised), which ConsToPrim touches as the reference's does.
     """
 
-    def __init__(self, cfg: MeshConfig, exact=False, device="cuda", face_fluxes=False,
+    def __init__(self, cfg: MeshConfig, exact=True, device="cuda", face_fluxes=False,
                  eos_lambda=False):
         require_cuda()
         _capi.load()
@@ -185,7 +185,7 @@ class Driver:
     clipped at tlim.
     """
 
-    def __init__(self, cfg: MeshConfig, cons0, exact=False, per_block=False):
+    def __init__(self, cfg: MeshConfig, cons0, exact=True, per_block=False):
         self.cfg = cfg
         self.md = MeshData(cfg, exact)
         self.per_block = per_block

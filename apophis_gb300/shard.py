@@ -218,7 +218,7 @@ class GpuShard:
     ghost cells filled by the halo exchange before each stage."""
 
     def __init__(self, cfg: MeshConfig, parts: List[List[int]], rank: int, cons_local,
-                 exact=False, tlim=None, group=None):
+                 exact=True, tlim=None, group=None):
         from . import _capi
         from .hydro import STAGES, stream_handle
         from .stepper import Stepper

@@ -22,7 +22,7 @@ TUNE_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "a
 
 
 class Stepper:
-    def __init__(self, cfg: MeshConfig, cons0=None, exact=False, tlim=None, fixed_dt=0.0,
+    def __init__(self, cfg: MeshConfig, cons0=None, exact=True, tlim=None, fixed_dt=0.0,
                  cons=None, dx=None):
         require_cuda()
         _capi.load()
