@@ -114,6 +114,7 @@ __device__ __forceinline__ double twice_x(double x) {
 // q1 -- the one with the smaller remainder -- is RN(x/6) (a tie would need x to have more
 // than 53 significant bits).  Valid for x zero or normal with 2^-1000 < |x| < 2^1000.
 __device__ __forceinline__ double div6_x(double x) {
+  if ((__double_as_longlong(x) << 1) == 0) return x;  // +-0 / 6 = +-0
   const double q0 = x * (1.0 / 6.0);
   const double r0 = fma(-6.0, q0, x);
   const long long b = __double_as_longlong(q0);
@@ -431,16 +432,33 @@ __device__ __forceinline__ void ppm_cell(double q_im2, double q_im1, double q_i,
     mx = a3 > mx ? a3 : mx;
     mx = a4 > mx ? a4 : mx;
     double rho = 0.0;
-    if (mag(d2qf) > mag(1.0e-12 * from_bits(mx))) rho = qe / d2qf;
-    if (le(rho, 1.0 - 1.0e-12)) {
+    const bool guard = mag(d2qf) > mag(1.0e-12 * from_bits(mx));
 #if APH_EXACT
-      qr = T ? sub_x(q_i, rho * dqf_minus) : q_i - rho * dqf_minus;
-      ql = T ? add_x(q_i, rho * dqf_plus) : q_i + rho * dqf_plus;
+    if (T && ((__double_as_longlong(qe) << 1) == 0 || !guard)) {
+      // rho is a zero (+0 without the guard, else qe / d2qf = +-0 by the signs): the products
+      // rho * dqf are zeros with the product of the signs, and no division is needed
+      const long long rs = guard ? ((__double_as_longlong(qe) ^ __double_as_longlong(d2qf)) &
+                                    (long long)0x8000000000000000ULL) : 0LL;
+      const double zm = __longlong_as_double(rs ^ (__double_as_longlong(dqf_minus) & (long long)0x8000000000000000ULL));
+      const double zp = __longlong_as_double(rs ^ (__double_as_longlong(dqf_plus) & (long long)0x8000000000000000ULL));
+      qr = sub_x(q_i, zm);
+      ql = add_x(q_i, zp);
+    } else if (T && __double_as_longlong(qe) == __double_as_longlong(d2qf)) {
+      // rho = d2qf / d2qf = 1 > 1 - 1e-12: the face values stay
+    } else {
+      if (guard) rho = qe / d2qf;
+      if (le(rho, 1.0 - 1.0e-12)) {
+        qr = T ? sub_x(q_i, rho * dqf_minus) : q_i - rho * dqf_minus;
+        ql = T ? add_x(q_i, rho * dqf_plus) : q_i + rho * dqf_plus;
+      }
+    }
 #else
+    if (guard) rho = qe / d2qf;
+    if (le(rho, 1.0 - 1.0e-12)) {
       qr = fma(-rho, dqf_minus, q_i);
       ql = fma(rho, dqf_plus, q_i);
-#endif
     }
+#endif
   } else {
     if (mag(dqf_minus) >= twice_mag(dqf_plus))
       qr = T ? sub_x(q_i, twice_x(dqf_plus)) : q_i - 2.0 * dqf_plus;
