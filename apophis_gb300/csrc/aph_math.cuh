@@ -106,22 +106,37 @@ __device__ __forceinline__ double twice_x(double x) {
   const long long b = __double_as_longlong(x);
   return (b << 1) == 0 ? x : __longlong_as_double(b + (1LL << 52));
 }
-// x / 6.0 correctly rounded, by the exact remainder (the method of Brisebarre, Muller and
-// Raina for a divisor known in advance, with the rounding decided by comparing remainders):
-// c = RN(1/6) has relative error exactly 2^-54, so q0 = RN(x c) is within one ulp of x/6
-// (faithful); then r0 = x - 6 q0 is exact (one fma), x/6 lies strictly between q0 and its
-// neighbour q1 on the side of r0's sign, r1 = x - 6 q1 is exact too, and the nearer of q0 and
-// q1 -- the one with the smaller remainder -- is RN(x/6) (a tie would need x to have more
-// than 53 significant bits).  Valid for x zero or normal with 2^-1000 < |x| < 2^1000.
+// x / 6.0 correctly rounded, on the integer pipe: with the significand M (leading 1 moved to
+// bit 63), floor(M / 3) is the high word of M * 0xAAAAAAAAAAAAAAAB shifted right once (the
+// exact quotient by an invariant divisor, Granlund and Montgomery), the remainder M - 3 floor
+// gives one more exact bit where the quotient is one bit short and a sticky bit, and the
+// quotient is rounded to nearest even (x / 6 is never a midpoint: a midpoint times 6 would need
+// more than 53 significant bits).  Valid for x zero or normal with 2^-1000 < |x| < 2^1000.
 __device__ __forceinline__ double div6_x(double x) {
-  if ((__double_as_longlong(x) << 1) == 0) return x;  // +-0 / 6 = +-0
-  const double q0 = x * (1.0 / 6.0);
-  const double r0 = fma(-6.0, q0, x);
-  const long long b = __double_as_longlong(q0);
-  const long long b1 = b + ((is_pos(r0) == is_pos(q0)) ? 1LL : -1LL);  // toward x/6 (q0 != 0)
-  const double q1 = __longlong_as_double(b1);
-  const double r1 = fma(-6.0, q1, x);
-  return ((b << 1) != 0 && mag(r1) < mag(r0)) ? q1 : q0;
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long mg = u & 0x7fffffffffffffffULL;
+  if (mg == 0) return x;  // +-0 / 6 = +-0
+  const unsigned long long N = ((mg & 0xfffffffffffffULL) | 0x10000000000000ULL) << 11;
+  const unsigned long long Q = __umul64hi(N, 0xAAAAAAAAAAAAAAABULL) >> 1;  // floor(N / 3)
+  const unsigned long long R = N - 3ULL * Q;                                 // 0, 1 or 2
+  unsigned long long V;
+  long long e = (long long)(mg >> 52);
+  if (Q >> 62) {  // leading 1 at bit 62
+    V = Q;
+    e -= 2;
+  } else {        // at bit 61: append the next exact bit of N / 3
+    V = 2ULL * Q + (R == 2ULL ? 1ULL : 0ULL);
+    e -= 3;
+  }
+  unsigned long long m = V >> 10;
+  const unsigned long long r = V & 0x3ffULL;
+  if (r > 0x200ULL || (r == 0x200ULL && (R != 0ULL || (m & 1ULL)))) ++m;
+  if (m >> 53) {
+    m >>= 1;
+    ++e;
+  }
+  return __longlong_as_double(
+      (long long)((u & 0x8000000000000000ULL) | ((unsigned long long)e << 52) | (m & 0xfffffffffffffULL)));
 }
 
 // ---- IEEE double additions and small multiplications on the integer pipe ---------------
@@ -432,7 +447,19 @@ __device__ __forceinline__ void ppm_cell(double q_im2, double q_im1, double q_i,
     mx = a3 > mx ? a3 : mx;
     mx = a4 > mx ? a4 : mx;
     double rho = 0.0;
-    const bool guard = mag(d2qf) > mag(1.0e-12 * from_bits(mx));
+    // the roundoff guard |d2qf| > 1e-12 * max|q| (ppm_simple.hpp:132); RN(1e-12 * mx) lies in
+    // [2^-40, 2^-38) times mx's binade, so the exponents decide it except within two binades
+    bool guard;
+    if (T) {
+      const long long ed = (long long)(mag(d2qf) >> 52), em = (long long)(mx >> 52);
+      if (mag(d2qf) == 0) guard = false;  // 0 > anything is false
+      else if (mx == 0) guard = true;      // a nonzero value over 1e-12 * 0
+      else if (ed >= em - 38) guard = true;
+      else if (ed <= em - 41) guard = false;
+      else guard = mag(d2qf) > mag(1.0e-12 * from_bits(mx));
+    } else {
+      guard = mag(d2qf) > mag(1.0e-12 * from_bits(mx));
+    }
 #if APH_EXACT
     if (T && ((__double_as_longlong(qe) << 1) == 0 || !guard)) {
       // rho is a zero (+0 without the guard, else qe / d2qf = +-0 by the signs): the products
