@@ -66,13 +66,13 @@ BYTES_PER_ZONE_UPDATE = 200.0   # RK2 with 5 FP64 conserved variables
 # FP64 work of the stage kernel per RK2 zone-update on this workload: the DADD + DMUL + DFMA
 # thread instructions the kernel executes (ncu sass counters of one stage launch of each kind
 # on a 128^3 pack of 64^3 blocks, per zone), by arithmetic mode
-FP64_LANE_OPS_PER_ZONE_UPDATE = {"fast": 1981.0, "exact": 3623.0}
+FP64_LANE_OPS_PER_ZONE_UPDATE = {"fast": 1981.0, "exact": 2487.0}
 FP64_LANES_PER_CLK_PER_SM = 2.0    # DFMA lanes per clock per SM on GB300 (measured)
 # DRAM bytes (read + write) per zone per stage launch, same captures (the 256^3 launches
 # process 8x the blocks of the 128^3 capture, so traffic is scaled by zones)
-TRAFFIC_BYTES_PER_ZONE_LAUNCH = {"fast": 628.3, "exact": 683.6}
+TRAFFIC_BYTES_PER_ZONE_LAUNCH = {"fast": 628.3, "exact": 689.1}
 TRAFFIC_LAUNCH = {"fast": "8 lines, dynamic schedule (not the tuned launch)",
-                  "exact": "256 threads, 6 lines, strided schedule: the tuned launch"}
+                  "exact": "256 threads, 3 lines, dynamic schedule, 80-register build: the tuned launch"}
 PARITY = {
     "exact": "bit-identical to the oracle (the reference's FP64 CPU path): one step of this "
              "256^3 pack with this launch, 50 steps of 128^3, the refined RT pack over 100 "
@@ -512,7 +512,7 @@ def timed_stepper(cfg, cons, exact, args, dist, local):
         c.update(json.loads(args.launch))
         st.set_config(c)
     elif not args.no_tune:
-        st.autotune(trial_steps=1)
+        st.autotune(trial_steps=2)  # two timed steps per candidate: a steadier choice
     stream = torch.cuda.current_stream()
     st.step(args.warmup)
     st.status()
