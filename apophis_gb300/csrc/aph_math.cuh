@@ -618,6 +618,17 @@ __device__ __forceinline__ double div_vol(double y, double vol, double ivol, boo
   return y / vol;
 }
 
+// The reference's c-limited sound speed C sqrt(gamma / (1 + (igm1 + rho C^2 / p)))
+// (hydro_hllc.hpp:57-60) with its roundings.  Where X = rho C^2 / p is at least 2^55 times
+// both igm1 and 1 (always for non-relativistic gas: X ~ (c_light / c_sound)^2), each addition
+// adds less than a quarter ulp of X and returns X, so both are skipped.
+__device__ __forceinline__ double csound_exact(double rho, double p, double gamma, double igm1) {
+  const double X = rho * C_LIGHT2 / p;
+  const long long ex = (long long)(mag(X) >> 52), ei = (long long)(mag(igm1) >> 52);
+  const double den = (ex >= 1023 + 55 && ex >= ei + 55 && ex < 2047) ? X : 1 + (igm1 + X);
+  return C_LIGHT * sqrt(gamma / den);
+}
+
 // exponent field all ones: an infinity or a NaN
 __device__ __forceinline__ bool nonfinite(double x) {
   return ((__double2hiint(x) >> 20) & 0x7ff) == 0x7ff;
@@ -644,8 +655,8 @@ __device__ __forceinline__ void solve_hllc_exact(const double *wli, const double
   auto hlf = [](double x) { return TAME ? half_x(x) : 0.5 * x; };
   const double gammal = glc, gammar = grc;
   const double igm1l = __drcp_rn(gle - 1), igm1r = __drcp_rn(gre - 1);  // == 1.0 / (g - 1)
-  const double cl = C_LIGHT * sqrt(gammal / (1 + (igm1l + wli[IDN] * C_LIGHT2 / wli[IPR])));
-  const double cr = C_LIGHT * sqrt(gammar / (1 + (igm1r + wri[IDN] * C_LIGHT2 / wri[IPR])));
+  const double cl = csound_exact(wli[IDN], wli[IPR], gammal, igm1l);
+  const double cr = csound_exact(wri[IDN], wri[IPR], gammar, igm1r);
   const double rhoa = hlf(wli[IDN] + wri[IDN]);
   const double ca = hlf(cl + cr);
   double pstar;
