@@ -31,7 +31,11 @@ __global__ void k_exact_ops2(int op, const double *x, const double *y, double *o
     else if (op == 1) r = sub_x(a, b);
     else if (op == 2) r = mulk_x<3, 0>(a);
     else if (op == 3) r = mulk_x<3, 1>(a);
-    else r = mulk_x<5, -2>(a);
+    else if (op == 4) r = mulk_x<5, -2>(a);
+    else if (op == 5) r = a / b;
+    else if (op == 6) r = __drcp_rn(b);
+    else if (op == 7) r = sqrt(a);
+    else r = div_rcp(a, b, __drcp_rn(b));
     out[i] = r;
   }
 }
@@ -41,7 +45,7 @@ __global__ void k_exact_ops2(int op, const double *x, const double *y, double *o
 extern "C" aph_status aph_diag_exact_ops2(int op, const double *x, const double *y, double *out,
                                           long long n, void *stream) {
   clear_error();
-  if (op < 0 || op > 4) return fail(APH_ERR_INVALID, "op %d not in 0..4", op);
+  if (op < 0 || op > 8) return fail(APH_ERR_INVALID, "op %d not in 0..8", op);
   if (n < 0 || (n > 0 && (!x || !y || !out))) return fail(APH_ERR_INVALID, "NULL argument");
   if (n == 0) return APH_OK;
   const long long blocks = (n + 255) / 256;

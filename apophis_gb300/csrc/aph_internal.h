@@ -96,15 +96,23 @@ struct MemberCtl {
   int ncycle, active;
 };
 
+// A pass item's lines: its first line and its line count share one int (count below
+// 2^kItemLineBits, first line below 2^(31 - kItemLineBits)).
+constexpr int kItemLineBits = 10;
+
 // Arguments of one stage launch.
 struct StageArgs {
   PackDev p;
   const StepBlock *blocks;
   StepCtl *ctl;
-  int *block_flags;             // per block: pressure floor applied somewhere in its cells
+  // per block b: [2b] the number of the last launch whose ConsToPrim applied a floor in b,
+  // [2b+1] of the last launch that deferred a floored interior write-back of b; then at
+  // [2 nblocks] the number of the last stage launch (numbers only grow, so a flag is current
+  // when it equals the launch's own number and nothing has to clear the flags)
+  unsigned long long *block_flags;
   const int2 *cell_items;       // (block, first cell) chunks of blockDim.x entire-domain cells
   int ncell_items;
-  const int2 *line_items[3];    // per direction: (block, first line) of T[d] lines
+  const int2 *line_items[3];    // per direction: (block, first line << kItemLineBits | lines)
   int nline_items[3];
   const int *fix_items;         // refined meshes: blocks with a finer neighbour
   int nfix_items;
@@ -120,8 +128,9 @@ struct StageArgs {
   int gravity;
   int copy_u1;                  // stage 1: u1 <- u0 (interior, after the floors)
   int last;                     // last stage: dt candidates of the new state
-  int init;                     // ghost fill + dt estimate only
+  int init;                     // dt estimate only
   int ghosts_given;             // the caller filled every ghost cell of u0: no ghost phase
+  int full_domain;              // ConsToPrim of every ghost cell, also those no pass reads
   int schedule;                 // 0 strided, 1 contiguous, 2 dynamic
   unsigned long long timeout_ns;
 };

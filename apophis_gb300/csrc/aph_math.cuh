@@ -98,6 +98,10 @@ __device__ __forceinline__ bool tame(double x) {
   const unsigned e = hi >> 20;  // biased exponent
   return (e - (1023u - 200u) <= 400u) || ((hi | (unsigned)__double2loint(x)) == 0u);
 }
+__device__ __forceinline__ bool tame_nz(double x) {  // tame and nonzero
+  const unsigned e = ((unsigned)__double2hiint(x) & 0x7fffffffu) >> 20;
+  return e - (1023u - 200u) <= 400u;
+}
 __device__ __forceinline__ double half_x(double x) {
   const long long b = __double_as_longlong(x);
   return (b << 1) == 0 ? x : __longlong_as_double(b - (1LL << 52));
@@ -241,6 +245,35 @@ __device__ __forceinline__ double eos_bulk_modulus(double gm1, double rho, doubl
   return lt(small, b) ? b : small;
 }
 
+// RN(a / b) given y = RN(1 / b), by Markstein's theorem (P. W. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res. Develop. 34(1),
+// 1990, Theorem 1): q = RN(a y) lies within one ulp of a / b, so the remainder a - b q is
+// exact (one fused multiply-add), and RN(q + (a - b q) y) is the correctly rounded quotient.
+// For a and b tame (b nonzero), where no product or remainder leaves the normal range; a zero
+// remainder means q = a / b exactly (and keeps the sign of a zero quotient).
+__device__ __forceinline__ double div_rcp(double a, double b, double y) {
+  const double q = __dmul_rn(a, y);
+  if ((((unsigned)__double2hiint(a) & 0x7fffffffu) | (unsigned)__double2loint(a)) == 0u) return q;
+  return __fma_rn(__fma_rn(-q, b, a), y, q);  // a nonzero: q nonzero, and q + (+-0) == q
+}
+
+// a / b correctly rounded, from y = RN(1 / b) where a and b allow it (the division otherwise).
+__device__ __forceinline__ double div_y(double a, double b, double y) {
+  return (tame(a) && tame_nz(b)) ? div_rcp(a, b, y) : a / b;
+}
+
+// a1 / b and a2 / b correctly rounded, sharing one reciprocal where the operands allow.
+__device__ __forceinline__ void div2(double a1, double a2, double b, double &q1, double &q2) {
+  if (tame(a1) && tame(a2) && tame_nz(b)) {
+    const double y = __drcp_rn(b);
+    q1 = div_rcp(a1, b, y);
+    q2 = div_rcp(a2, b, y);
+  } else {
+    q1 = a1 / b;
+    q2 = a2 / b;
+  }
+}
+
 // The reference's ConsToPrim arithmetic after the density floor (hydro.cpp:502-531), one
 // rounded operation at a time in its order: the fast build contracts products and sums into
 // FMAs, and these values must match the reference bit for bit where they feed the
@@ -254,7 +287,7 @@ __device__ __forceinline__ bool cons_to_prim_tail(double *u, double *w, double &
   const double e_k = __dmul_rn(__dmul_rn(0.5, di),
                                __dadd_rn(__dadd_rn(__dmul_rn(m1, m1), __dmul_rn(m2, m2)), __dmul_rn(m3, m3)));
   double u_e = u[IEN];
-  double sie = __ddiv_rn(__dsub_rn(u_e, e_k), u_d);  // (u_e - e_k) / u_d
+  double sie = div_y(__dsub_rn(u_e, e_k), u_d, di);  // (u_e - e_k) / u_d
   double w_p = __dmul_rn(__dmul_rn(gm1, u_d), sie);
   w_p = is_neg(w_p) ? 0.0 : w_p;  // eos_pressure
   const bool floored = !gt(w_p, pfloor);
@@ -262,7 +295,7 @@ __device__ __forceinline__ bool cons_to_prim_tail(double *u, double *w, double &
     const double gm1q = __ddiv_rn(w_p, __dmul_rn(u_d, e_k));  // hydro.cpp:517
     u_e = __dadd_rn(__ddiv_rn(pfloor, gm1q), e_k);
     w_p = pfloor;
-    sie = __ddiv_rn(__dsub_rn(u_e, e_k), u_d);  // of the floored energy (unchanged otherwise)
+    sie = div_y(__dsub_rn(u_e, e_k), u_d, di);  // of the floored energy (unchanged otherwise)
   }
   u[IEN] = u_e;
   w[IPR] = w_p;
@@ -280,7 +313,8 @@ __device__ __forceinline__ bool cons_to_prim_tail(double *u, double *w, double &
 __device__ __forceinline__ bool cons_to_prim_cell(double *u, double *w, double &g_c, double &g_e,
                                                   double gm1, double dfloor, double pfloor) {
   double u_d = u[IDN];
-  u_d = gt(u_d, dfloor) ? u_d : dfloor;
+  const bool dens_ok = gt(u_d, dfloor);
+  u_d = dens_ok ? u_d : dfloor;
   u[IDN] = u_d;
   const double di = __drcp_rn(u_d);  // the correctly rounded 1.0 / u_d
   w[IDN] = u_d;
@@ -290,7 +324,8 @@ __device__ __forceinline__ bool cons_to_prim_cell(double *u, double *w, double &
 #if !APH_EXACT
   // fast: p = gm1 rho ((E - e_k) / rho) = gm1 (E - e_k), and with the floors inactive both
   // adiabatic indices are gamma (B / p = gm1 + 1 = p / (rho e) + 1), so one division per cell
-  {
+  // (a floored density takes the reference's arithmetic below, whose indices are kept)
+  if (dens_ok) {
     const double e_k = 0.5 * di * (u[IM1] * u[IM1] + u[IM2] * u[IM2] + u[IM3] * u[IM3]);
     const double pe = gm1 * (u[IEN] - e_k);
     const double wp = is_neg(pe) ? 0.0 : pe;
@@ -622,8 +657,8 @@ __device__ __forceinline__ double div_vol(double y, double vol, double ivol, boo
 // (hydro_hllc.hpp:57-60) with its roundings.  Where X = rho C^2 / p is at least 2^55 times
 // both igm1 and 1 (always for non-relativistic gas: X ~ (c_light / c_sound)^2), each addition
 // adds less than a quarter ulp of X and returns X, so both are skipped.
-__device__ __forceinline__ double csound_exact(double rho, double p, double gamma, double igm1) {
-  const double X = rho * C_LIGHT2 / p;
+__device__ __forceinline__ double csound_exact(double rho, double p, double gamma, double igm1, double yp) {
+  const double X = div_y(rho * C_LIGHT2, p, yp);
   const long long ex = (long long)(mag(X) >> 52), ei = (long long)(mag(igm1) >> 52);
   const double den = (ex >= 1023 + 55 && ex >= ei + 55 && ex < 2047) ? X : 1 + (igm1 + X);
   return C_LIGHT * sqrt(gamma / den);
@@ -655,8 +690,11 @@ __device__ __forceinline__ void solve_hllc_exact(const double *wli, const double
   auto hlf = [](double x) { return TAME ? half_x(x) : 0.5 * x; };
   const double gammal = glc, gammar = grc;
   const double igm1l = __drcp_rn(gle - 1), igm1r = __drcp_rn(gre - 1);  // == 1.0 / (g - 1)
-  const double cl = csound_exact(wli[IDN], wli[IPR], gammal, igm1l);
-  const double cr = csound_exact(wri[IDN], wri[IPR], gammar, igm1r);
+  // 1 / p of each side: the sound speed and the shock factor divide by p (div_y; unused
+  // where the operands leave the tame range and the divisions are made as such)
+  const double ypl = __drcp_rn(wli[IPR]), ypr = __drcp_rn(wri[IPR]);
+  const double cl = csound_exact(wli[IDN], wli[IPR], gammal, igm1l, ypl);
+  const double cr = csound_exact(wri[IDN], wri[IPR], gammar, igm1r, ypr);
   const double rhoa = hlf(wli[IDN] + wri[IDN]);
   const double ca = hlf(cl + cr);
   double pstar;
@@ -673,10 +711,10 @@ __device__ __forceinline__ void solve_hllc_exact(const double *wli, const double
   const bool bl = gt(pstar, wli[IPR]), br = gt(pstar, wri[IPR]);
   if (bl || br) {
     const double k = (gammal + 1) / (TAME ? twice_x(gammar) : 2 * gammar);
-    const double q1 = sqrt(1.0 + k * (pstar / (bl ? wli[IPR] : wri[IPR]) - 1.0));
+    const double q1 = sqrt(1.0 + k * (div_y(pstar, bl ? wli[IPR] : wri[IPR], bl ? ypl : ypr) - 1.0));
     if (bl) ql = q1;
     else qr = q1;
-    if (bl && br) qr = sqrt(1.0 + k * (pstar / wri[IPR] - 1.0));
+    if (bl && br) qr = sqrt(1.0 + k * (div_y(pstar, wri[IPR], ypr) - 1.0));
   }
   const double sl = wli[IV1] - cl * ql;
   const double sr = wri[IV1] + cr * qr;
@@ -688,13 +726,13 @@ __device__ __forceinline__ void solve_hllc_exact(const double *wli, const double
   const double tr = wri[IPR] + vxr0 * wri[IDN] * wri[IV1];
   const double ml = wli[IDN] * vxl0;
   const double mr = -(wri[IDN] * vxr0);
-  const double sstar = (tl - tr) / (ml + mr);
-  double cp = (ml * tr + mr * tl) / (ml + mr);
+  double sstar, cp;  // (tl - tr) / (ml + mr), (ml tr + mr tl) / (ml + mr)
+  div2(tl - tr, ml * tr + mr * tl, ml + mr, sstar, cp);
   cp = is_pos(cp) ? cp : 0.0;
   const bool L = !is_neg(sstar);  // sstar >= 0.0
   const double den = L ? sstar - bm : bp - sstar;
-  const double coef = (L ? sstar : -sstar) / den;  // ul, or ur
-  const double ustar = (L ? -bm : bp) / den;
+  double coef, ustar;  // ul (or ur) and ustar: (+-sstar) / den, (-bm or bp) / den
+  div2(L ? sstar : -sstar, L ? -bm : bp, den, coef, ustar);
   // the upwind side (U) and the other one (O)
   const double *wu = L ? wli : wri, *wo = L ? wri : wli;
   const double igu = L ? igm1l : igm1r;
@@ -900,8 +938,9 @@ __device__ __forceinline__ double dt_candidate(const double *w, double e_cons, c
   const double e_internal =
       (e_cons - 0.5 * w[IDN] * (w[IV1] * w[IV1] + w[IV2] * w[IV2] + w[IV3] * w[IV3])) / w[IDN];
   const double bulkmod = eos_bulk_modulus(gm1, w[IDN], e_internal);
-  const double gamma_c = bulkmod / w[IPR];
-  const double lam = C_LIGHT * sqrt(gamma_c / (1 + (e_internal + C_LIGHT2) * w[IDN] / w[IPR]));
+  double gamma_c, rat;  // bulkmod / p, (e_internal + c^2) rho / p
+  div2(bulkmod, (e_internal + C_LIGHT2) * w[IDN], w[IPR], gamma_c, rat);
+  const double lam = C_LIGHT * sqrt(gamma_c / (1 + rat));
   double m = dx[0] / (dabs(w[IV1]) + lam);
   if (ndim > 1) {
     const double c2 = dx[1] / (dabs(w[IV2]) + lam);

@@ -2,14 +2,16 @@
 // meshblock of a pack, uneven block sizes included.
 //
 // Phases, separated by a grid-wide barrier whose waits are bounded in time:
-//   0  ghost zones of u0 from the neighbours' interiors and the physical boundaries
-//   1  ConsToPrim of u0 over the entire domain (floors applied to u0 in place, prim and
-//      gamma to scratch); at stage 1 the floored interior is copied to u1
+//   1  per cell of the entire domain: a ghost cell's values from the neighbours' interiors
+//      and the physical boundaries, then ConsToPrim (floors applied to u0, prim and gamma
+//      to scratch); at stage 1 the floored interior is copied to u1
 //   2+ one pass per direction: stage prim lines in shared memory, PPM with each face
 //      value computed once and shared by its two cells (or PLM / donor cell), Riemann
 //      solve, flux difference; the directions' differences accumulate in du in the
 //      reference's x, y, z order, and the last pass applies the RK update,
-//      the constant-g source and, at the last stage, the dt candidate of the new state.
+//      the constant-g source and, at the last stage, the dt candidate of the new state
+//   +  refined meshes only: the coarse cells at coarse-fine faces, corrected and updated
+//      once every block's face fluxes are kept
 // Face states live in shared memory only.  On GB300 the FP64 pipe, not HBM, bounds this
 // kernel, so the design aims at the least FP64 work per zone: no reconstruction of
 // ghost rows, one evaluation per face value, constant adiabatic indices when no floor
@@ -156,7 +158,7 @@ struct Sched {
   }
 };
 
-// ---- phase 0: ghost fill on a uniform block grid -------------------------------------
+// ---- ghost values on a uniform block grid ---------------------------------------------
 __device__ __forceinline__ int map_index(int g, int n, int lo, int hi, bool &flip) {
   if (g < 0) {
     if (lo == 0) return g + n;      // periodic
@@ -182,6 +184,9 @@ __device__ __forceinline__ int map_index(int g, int n, int lo, int hi, bool &fli
 // floor (eraw) and after it (efl).  The first stage of the next step reads the energy before
 // the floor wherever the stored energy is still the floored one, so the floor is applied once.
 constexpr unsigned long long kNoFloorTag = ~0ULL;  // a NaN that arithmetic never produces
+// Marks (in a cell's du slot of the first momentum) a floored density and energy waiting in
+// its du slots of those components; another NaN that arithmetic never produces.
+constexpr unsigned long long kDeferTag = ~1ULL;
 
 __device__ __forceinline__ double energy_in(const StepBlock &X, long long c, bool step_start) {
   const double e = X.u0[IEN * X.ncell + c];
@@ -237,6 +242,23 @@ __device__ __forceinline__ bool is_interior(const PackDev &p, const StepBlock &B
   return in;
 }
 
+// Whether a pass reads ghost cell (i, j, k) of B: outside the interior along exactly one
+// direction, by at most G cells.
+__device__ __forceinline__ bool pass_reads(const PackDev &p, const StepBlock &B, int i, int j, int k,
+                                           int G) {
+  const int e[3] = {i, j, k};
+  int out = 0, depth = 0;
+  for (int d = 0; d < p.ndim; ++d) {
+    const int x = e[d] - p.ng;
+    const int o = x < 0 ? -x : (x >= B.nx[d] ? x - B.nx[d] + 1 : 0);
+    if (o > 0) {
+      ++out;
+      depth = o;
+    }
+  }
+  return out == 1 && depth <= G;
+}
+
 __device__ __forceinline__ unsigned long long block_min(unsigned long long v) {
   __shared__ unsigned long long red[32];
 #pragma unroll
@@ -288,6 +310,24 @@ __device__ __forceinline__ void member_min(const StageArgs &a, int member, unsig
     v = x < v ? x : v;
   }
   if ((threadIdx.x & 31) == 0 && v != ~0ULL) atomicMin(&a.members[member].min_bits, v);
+}
+
+// ---- refined meshes: the cells the coarse-fine correction changes ----------------------
+// Bit f set: face f (x-, x+, y-, y+) of B has a finer neighbour.
+template <class BLK>
+__device__ __forceinline__ int amr_finer_mask(const BLK &B) {
+  int m = 0;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) m |= (B.amr.kind[f] == FACE_FINER ? 1 : 0) << f;
+  return m;
+}
+
+// Whether interior cell ic (x fastest) of a 2D block lies on a face of the mask.
+template <class BLK>
+__device__ __forceinline__ bool amr_defers(int fmask, const BLK &B, long long ic) {
+  const int j = (int)(ic / B.nx[0]), i = (int)(ic - (long long)j * B.nx[0]);
+  return ((fmask & 1) && i == 0) || ((fmask & 2) && i == B.nx[0] - 1) ||
+         ((fmask & 4) && j == 0) || ((fmask & 8) && j == B.nx[1] - 1);
 }
 
 // ---- line geometry of a pass ----------------------------------------------------------
@@ -410,7 +450,7 @@ __device__ __forceinline__ void ppm_window(const double *W, double *D2, double *
 // already APH_ERR_TIMEOUT and whose results are invalid.
 template <int DIR, int RECON, int RS>
 __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0, int nl, int T,
-                          bool constg, bool first_pass, bool last_pass, double *sm,
+                          bool constg, bool deferred, bool first_pass, bool last_pass, double *sm,
                           unsigned long long &dtmin, unsigned mbar, unsigned &tma_phase) {
   constexpr int G = Halo<RECON>::G;
   const int n = B.nx[DIR - 1];
@@ -493,8 +533,10 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
         x = B.gamma[(v - nv) * nc + cell];
 #else
         // the fast ConsToPrim leaves the constants where no floor fired; the reference's
-        // values (which the limiters see) are recomputed from the cell's state there
-        if (__double_as_longlong(B.prim[IPR * nc + cell]) == __double_as_longlong(a.p.pfloor)) {
+        // values (which the limiters see) are recomputed from the cell's state there (a
+        // floored cell's state may still wait in du for the first pass to store it)
+        if (__double_as_longlong(B.prim[IPR * nc + cell]) == __double_as_longlong(a.p.pfloor) ||
+            __double_as_longlong(B.prim[IDN * nc + cell]) == __double_as_longlong(a.p.dfloor)) {
           x = B.gamma[(v - nv) * nc + cell];  // floored: the reference's values already
         } else {
           double uc[NHYDRO], g_c, g_e;
@@ -595,12 +637,25 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
           F[v * fs + (size_t)t * w1 + (side == 0 ? 0 : n)];
     }
   }
+  if (deferred) {  // first pass: store the floored interior values ConsToPrim left in du
+    for (int it = tid; it < nl * n; it += nth) {
+      const int t = it / n, c = it - t * n;
+      long long base, stride, ib, is;
+      line_of<DIR>(B, a.p.ndim, a.p.ng, l0 + t, base, stride, ib, is);
+      const long long icell = ib + c * is;
+      if (__double_as_longlong(B.du[IM1 * B.nint + icell]) == (long long)kDeferTag) {
+        B.u0[IDN * nc + base + c * stride] = B.du[IDN * B.nint + icell];
+        B.u0[IEN * nc + base + c * stride] = B.du[IEN * B.nint + icell];
+      }
+    }
+    __syncthreads();
+  }
   // F: flux difference of each interior cell; du accumulates x, y, z in order
   {
     const int w1 = n + 1;
     const size_t fs = (size_t)T * w1;
     const double area = DIR == 1 ? B.dx[1] * B.dx[2] : DIR == 2 ? B.dx[0] * B.dx[2] : B.dx[0] * B.dx[1];
-    if (!last_pass || a.cf) {
+    if (!last_pass) {
       for (int it = tid; it < nv * nl * n; it += nth) {
         const int v = it / (nl * n);
         const int r = it - v * nl * n;
@@ -619,6 +674,7 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
       const bool vol_p2 = pow2_normal(vol);  // power-of-two volume: exact multiplication
 #endif
       const double beta_dt = a.beta * dt_of(a, B);
+      const int fmask = a.cf ? amr_finer_mask(B) : 0;
       unsigned long long mymin = ~0ULL;
       for (int it = tid; it < nl * n; it += nth) {
         const int t = it / n, c = it - t * n;
@@ -626,6 +682,17 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
         line_of<DIR>(B, a.p.ndim, a.p.ng, l0 + t, base, stride, ib, is);
         const long long cell = base + c * stride;
         const long long icell = ib + c * is;
+        if (fmask && amr_defers(fmask, B, icell)) {
+          // a coarse cell at a face with a finer neighbour: its flux difference waits for
+          // the correction, and amr_fix updates it
+          for (int v = 0; v < nv; ++v) {
+            const size_t of = v * fs + (size_t)t * w1 + c;
+            const double d = (area * F[of + 1] - area * F[of]);
+            double *du = B.du + v * B.nint + icell;
+            *du = first_pass ? d : *du + d;
+          }
+          continue;
+        }
         double u[NHYDRO];
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v) {
@@ -692,87 +759,96 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
   return true;
 }
 
-// Refined meshes: conservation at coarse-fine faces.  Each coarse block with a finer
-// neighbour corrects its boundary cells' flux differences from its own face flux to the mean
-// of the fine face fluxes, faces in the order x-, x+, y-, y+.
-__device__ void amr_correct(const StageArgs &a, const Sched &sched, unsigned int *ctr) {
-  for (int it = sched.first(ctr, a.nfix_items); it < a.nfix_items; it = sched.next(ctr, a.nfix_items, it)) {
-    const StepBlock &B = a.blocks[a.fix_items[it]];
-    for (int face = 0; face < 4; ++face) {
-      if (B.amr.kind[face] != FACE_FINER) continue;
-      const int d = face / 2, s = face % 2, td = 1 - d;
-      const double area = d == 0 ? B.dx[1] * B.dx[2] : B.dx[0] * B.dx[2];
-      const int nv = a.p.nvar;
-      for (int it2 = threadIdx.x; it2 < B.nx[td] * nv; it2 += blockDim.x) {
-        const int t = it2 / nv, v = it2 % nv;
-        const int tg2 = 2 * (B.amr.origin[td] + t);
-        const StepBlock &F = amr_fine_nbr(a.blocks, B, face, td, tg2);
-        const int ft = tg2 - F.amr.origin[td];
-        const double *fb = F.bflux + (size_t)(2 * d + 1 - s) * a.bflux_stride;
-        const double Fold = B.bflux[(size_t)face * a.bflux_stride + (size_t)t * nv + v];
-        const double Fnew = 0.5 * (fb[(size_t)ft * nv + v] + fb[(size_t)(ft + 1) * nv + v]);
-        const int ca = s == 0 ? 0 : B.nx[d] - 1;
-        const int i = d == 0 ? ca : t, j = d == 0 ? t : ca;
-        double &x = B.du[v * B.nint + (long long)j * B.nx[0] + i];
-        x = s == 0 ? x + (area * Fold - area * Fnew) : x + (area * Fnew - area * Fold);
-      }
-      __syncthreads();
-    }
+// Refined meshes, after the last pass: the boundary cells of the coarse blocks at faces with
+// a finer neighbour (the cells the last pass left).  Each such cell's accumulated flux
+// difference takes, for every face of that kind it lies on (in the order x-, x+, y-, y+),
+// its own face flux replaced by the mean of the two fine face fluxes; then the RK update,
+// gravity and the dt candidate follow as in the last pass.
+__device__ __forceinline__ double amr_fixed_du(const StageArgs &a, const StepBlock &B, int fmask, int i,
+                                               int j, long long ic, int v) {
+  const int nv = a.p.nvar;
+  double x = B.du[v * B.nint + ic];
+  for (int face = 0; face < 4; ++face) {
+    if (!((fmask >> face) & 1)) continue;
+    const int d = face / 2, s = face % 2, td = 1 - d;
+    if ((d == 0 ? i : j) != (s == 0 ? 0 : B.nx[d] - 1)) continue;
+    const int t = d == 0 ? j : i;
+    const double area = d == 0 ? B.dx[1] * B.dx[2] : B.dx[0] * B.dx[2];
+    const int tg2 = 2 * (B.amr.origin[td] + t);
+    const StepBlock &F = amr_fine_nbr(a.blocks, B, face, td, tg2);
+    const int ft = tg2 - F.amr.origin[td];
+    const double *fb = F.bflux + (size_t)(2 * d + 1 - s) * a.bflux_stride;
+    const double Fold = B.bflux[(size_t)face * a.bflux_stride + (size_t)t * nv + v];
+    const double Fnew = 0.5 * (fb[(size_t)ft * nv + v] + fb[(size_t)(ft + 1) * nv + v]);
+    x = s == 0 ? x + (area * Fold - area * Fnew) : x + (area * Fnew - area * Fold);
   }
+  return x;
 }
 
-// Refined meshes: the RK update, gravity and dt candidates after the correction.
-__device__ void amr_update(const StageArgs &a, const Sched &sched, unsigned int *ctr,
-                           unsigned long long &dtmin) {
+__device__ void amr_fix(const StageArgs &a, const Sched &sched, unsigned int *ctr,
+                        unsigned long long &dtmin) {
   const PackDev &p = a.p;
-  const double beta_dt = a.beta * a.ctl->dt;
-  for (int it = sched.first(ctr, a.ncell_items); it < a.ncell_items; it = sched.next(ctr, a.ncell_items, it)) {
-    const int2 w = a.cell_items[it];
-    const StepBlock &B = a.blocks[w.x];
-    const long long c = (long long)w.y + threadIdx.x;
-    if (c >= B.ncell) continue;
-    int i, j, k;
-    if (!is_interior(p, B, c, i, j, k)) continue;
+  for (int it = sched.first(ctr, a.nfix_items); it < a.nfix_items; it = sched.next(ctr, a.nfix_items, it)) {
+    const StepBlock &B = a.blocks[a.fix_items[it]];
+    const int fmask = amr_finer_mask(B);
+    const GasConsts gc = gas_of(a, B);
+    const double beta_dt = a.beta * dt_of(a, B);
     const long long nc = B.ncell;
-    const long long ic = (long long)(j - p.ng) * B.nx[0] + (i - p.ng);
     const double vol = B.dx[0] * B.dx[1] * B.dx[2];
     const double ivol = 1.0 / vol;
+#if APH_EXACT
     const bool vol_p2 = pow2_normal(vol);  // power-of-two volume: exact multiplication
-    double u[NHYDRO];
+#endif
+    for (long long ic = threadIdx.x; ic < B.nint; ic += blockDim.x) {
+      if (!amr_defers(fmask, B, ic)) continue;
+      const int j = (int)(ic / B.nx[0]), i = (int)(ic - (long long)j * B.nx[0]);
+      const long long c = (long long)(j + p.ng) * B.ni + (i + p.ng);
+      double u[NHYDRO];
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v) {
-      const double div = div_vol(-B.du[v * B.nint + ic], vol, ivol, vol_p2);
-      u[v] = a.gam0 * B.u0[v * nc + c] + a.gam1 * B.u1[v * nc + c] + beta_dt * div;
-    }
-    bool bad = false;
-    for (int v = NHYDRO; v < p.nvar; ++v) {  // passive scalars
-      const double div = div_vol(-B.du[v * B.nint + ic], vol, ivol, vol_p2);
-      const double x = a.gam0 * B.u0[v * nc + c] + a.gam1 * B.u1[v * nc + c] + beta_dt * div;
-      B.u0[v * nc + c] = x;
-      bad |= ((__double_as_longlong(x) >> 52) & 0x7ff) == 0x7ff;
-    }
-    if (a.gravity) {
-      const double rho = B.prim[IDN * nc + c];
-      u[IM1] += a.grav[0] * rho * beta_dt;
-      double de = a.grav[0] * B.prim[IV1 * nc + c];
-      u[IM2] += a.grav[1] * rho * beta_dt;
-      de += a.grav[1] * B.prim[IV2 * nc + c];
-      u[IEN] += de * rho * beta_dt;
-    }
+      for (int v = 0; v < NHYDRO; ++v) {
+        const double du = amr_fixed_du(a, B, fmask, i, j, ic, v);
+#if APH_EXACT
+        const double div = div_vol(-du, vol, ivol, vol_p2);
+#else
+        const double div = -du * ivol;
+#endif
+        u[v] = a.gam0 * B.u0[v * nc + c] + a.gam1 * B.u1[v * nc + c] + beta_dt * div;
+      }
+      bool bad = false;
+      for (int v = NHYDRO; v < p.nvar; ++v) {  // passive scalars
+        const double du = amr_fixed_du(a, B, fmask, i, j, ic, v);
+#if APH_EXACT
+        const double div = div_vol(-du, vol, ivol, vol_p2);
+#else
+        const double div = -du * ivol;
+#endif
+        const double x = a.gam0 * B.u0[v * nc + c] + a.gam1 * B.u1[v * nc + c] + beta_dt * div;
+        B.u0[v * nc + c] = x;
+        bad |= ((__double_as_longlong(x) >> 52) & 0x7ff) == 0x7ff;
+      }
+      if (a.gravity) {  // ApplyGravity with the stage input's prim (gravity.cpp:386-407)
+        const double rho = B.prim[IDN * nc + c];
+        u[IM1] += a.grav[0] * rho * beta_dt;
+        double de = a.grav[0] * B.prim[IV1 * nc + c];
+        u[IM2] += a.grav[1] * rho * beta_dt;
+        de += a.grav[1] * B.prim[IV2 * nc + c];
+        u[IEN] += de * rho * beta_dt;
+      }
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v)
-      bad |= ((__double_as_longlong(u[v]) >> 52) & 0x7ff) == 0x7ff;  // NaN or inf
-    if (bad) a.ctl->nonfinite = 1;
-    if (a.last) {  // dt of the floored new state, which is stored floored (as in pass_item)
-      double wv[NHYDRO], gcc, gce;
-      const double e_raw = u[IEN];
-      cons_to_prim_cell(u, wv, gcc, gce, p.gm1, p.dfloor, p.pfloor);
-      const unsigned long long b = dt_bits(dt_candidate(wv, u[IEN], B.dx, p.ndim, p.gm1));
-      dtmin = b < dtmin ? b : dtmin;
-      store_floored_energy(B, c, e_raw, u[IEN]);
-    }
+      for (int v = 0; v < NHYDRO; ++v)
+        bad |= ((__double_as_longlong(u[v]) >> 52) & 0x7ff) == 0x7ff;  // NaN or inf
+      if (bad) a.ctl->nonfinite = 1;
+      if (a.last) {  // dt of the floored new state, which is stored floored (as in pass_item)
+        double wv[NHYDRO], gcc, gce;
+        const double e_raw = u[IEN];
+        const bool fl = cons_to_prim_cell(u, wv, gcc, gce, gc.gm1, p.dfloor, p.pfloor);
+        const unsigned long long b = dt_bits(dt_cell(wv, u[IEN], B.dx, p.ndim, gc, fl));
+        dtmin = b < dtmin ? b : dtmin;
+        store_floored_energy(B, c, e_raw, u[IEN]);
+      }
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + c] = u[v];
+      for (int v = 0; v < NHYDRO; ++v) B.u0[v * nc + c] = u[v];
+    }
   }
 }
 
@@ -793,33 +869,15 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
   unsigned long long dtmin = ~0ULL;
   unsigned int *ctr = a.ctl->work;
 
-  // phase 0: ghost zones (unless the caller filled them, e.g. by a halo exchange)
-  for (int it = a.ghosts_given ? a.ncell_items : sched.first(ctr + 0, a.ncell_items);
-       it < a.ncell_items; it = sched.next(ctr + 0, a.ncell_items, it)) {
-    const int2 w = a.cell_items[it];
-    const StepBlock &B = a.blocks[w.x];
-    if (!active_of(a, B)) continue;
-    const long long c = (long long)w.y + threadIdx.x;
-    if (c < B.ncell) {
-      if (p.amr) {
-        const bool start = a.copy_u1;
-        amr_fill_cell(
-            a.blocks, B,
-            [start](const StepBlock &X, int v, long long i) {
-              return v == IEN ? energy_in(X, i, start) : X.u0[v * X.ncell + i];
-            },
-            B.u0, p.nvar, p.bc, p.ng, c);
-      }
-      else
-        ghost_cell(a, B, c);
-    }
-  }
-  if (!a.init)
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < p.nblocks; b += gridDim.x * blockDim.x)
-      a.block_flags[b] = 0;
-  if (!grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
+  // this launch's number (read by every CTA before the first barrier, advanced after it)
+  const unsigned long long epoch = *(volatile unsigned long long *)&a.block_flags[2 * p.nblocks] + 1;
 
-  // phase 1: ConsToPrim (in init mode only the dt estimate, nothing is written)
+  // phase 1: per cell, its ghost values (from the neighbours' interiors and the physical
+  // boundaries, unless the caller filled them, e.g. by a halo exchange), then ConsToPrim.
+  // Ghost cells are floored in place.  Other blocks read interior cells for their ghosts
+  // during this phase, so a floored interior cell's density and energy wait in its du slots
+  // (tagged) until the first pass stores them.  In init mode only the dt estimate of the
+  // interior is made and nothing is written.
   for (int it = sched.first(ctr + 1, a.ncell_items); it < a.ncell_items;
        it = sched.next(ctr + 1, a.ncell_items, it)) {
     const int2 w = a.cell_items[it];
@@ -843,6 +901,24 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
       continue;
     }
     if (c >= B.ncell) continue;
+    int i, j, k;
+    const bool inner = is_interior(p, B, c, i, j, k);
+    // the passes read ghost cells only along their lines, at most G cells beyond the interior:
+    // the others (edges, corners, the layers beyond G) are neither filled nor converted
+    if (!inner && !a.full_domain && !pass_reads(p, B, i, j, k, Halo<RECON>::G)) continue;
+    if (!inner && !a.ghosts_given) {  // the ghost values of u0 (read back below by this thread)
+      if (p.amr) {
+        const bool start = a.copy_u1;
+        amr_fill_cell(
+            a.blocks, B,
+            [start](const StepBlock &X, int v, long long q) {
+              return v == IEN ? energy_in(X, q, start) : X.u0[v * X.ncell + q];
+            },
+            B.u0, p.nvar, p.bc, p.ng, c);
+      } else {
+        ghost_cell(a, B, c);
+      }
+    }
     const long long nc = B.ncell;
     double u[NHYDRO], wv[NHYDRO], g_c, g_e;
 #pragma unroll
@@ -850,10 +926,19 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
     const double ud0 = u[IDN], ue0 = u[IEN];
     u[IEN] = energy_in(B, c, a.copy_u1);
     const bool fl = cons_to_prim_cell(u, wv, g_c, g_e, gm1, p.dfloor, p.pfloor);
-    int i, j, k;
-    const bool inner = is_interior(p, B, c, i, j, k);
-    if (__double_as_longlong(u[IDN]) != __double_as_longlong(ud0)) B.u0[IDN * nc + c] = u[IDN];
-    if (__double_as_longlong(u[IEN]) != __double_as_longlong(ue0)) B.u0[IEN * nc + c] = u[IEN];
+    const bool changed = __double_as_longlong(u[IDN]) != __double_as_longlong(ud0) ||
+                         __double_as_longlong(u[IEN]) != __double_as_longlong(ue0);
+    if (changed && !inner) {
+      B.u0[IDN * nc + c] = u[IDN];
+      B.u0[IEN * nc + c] = u[IEN];
+    } else if (changed) {
+      const int sj = p.ndim >= 2 ? p.ng : 0, sk = p.ndim >= 3 ? p.ng : 0;
+      const long long ic = ((long long)(k - sk) * B.nx[1] + (j - sj)) * B.nx[0] + (i - p.ng);
+      B.du[IDN * B.nint + ic] = u[IDN];
+      B.du[IEN * B.nint + ic] = u[IEN];
+      B.du[IM1 * B.nint + ic] = __longlong_as_double((long long)kDeferTag);
+      a.block_flags[2 * w.x + 1] = epoch;
+    }
 #pragma unroll
     for (int n = 0; n < NHYDRO; ++n) B.prim[n * nc + c] = wv[n];
     B.gamma[c] = g_c;
@@ -866,7 +951,7 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
         if (a.copy_u1 && inner) B.u1[n * nc + c] = q;
       }
     }
-    if (fl) atomicOr(&a.block_flags[w.x], 1);
+    if (fl) a.block_flags[2 * w.x] = epoch;
     if (a.copy_u1 && inner) {
 #pragma unroll
       for (int n = 0; n < NHYDRO; ++n) B.u1[n * nc + c] = u[n];
@@ -878,6 +963,7 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
     return;
   }
   if (!grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.block_flags[2 * p.nblocks] = epoch;
 
   // phases 2..: one pass per direction
   for (int pi = 0; pi < p.ndim; ++pi) {
@@ -889,37 +975,37 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
       const int2 w = a.line_items[dir - 1][it];
       const StepBlock &B = a.blocks[w.x];
       if (!active_of(a, B)) continue;
-      const int ntrans = dir == 1 ? B.nx[1] * B.nx[2] : dir == 2 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1];
-      const int nl = min(T, ntrans - w.y);
+      const int lfirst = w.y >> kItemLineBits, nl = w.y & ((1 << kItemLineBits) - 1);
+      // shared-memory layout: the TMA box's lines, else the item's own
+      const int Ti = a.tmaps ? T : nl;
 #if APH_EXACT
       const bool constg = false;
 #else
-      const bool constg = a.block_flags[w.x] == 0;
+      const bool constg = a.block_flags[2 * w.x] != epoch;
 #endif
+      const bool deferred = first_pass && a.block_flags[2 * w.x + 1] == epoch;
       // the item's lines, in chunks that fit the gamma slabs where they are reconstructed
-      const int Tc = constg ? T : split_lines(T, p.nvar);
+      const int Tc = constg ? Ti : split_lines(Ti, p.nvar);
       for (int o = 0; o < nl; o += Tc) {
-        const int l0 = w.y + o, nc = min(Tc, nl - o);
+        const int l0 = lfirst + o, nc = min(Tc, nl - o);
         bool ok;
         if (dir == 1)
-          ok = pass_item<1, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin,
+          ok = pass_item<1, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, deferred, first_pass, last_pass, sm, dtmin,
                                        mbar, tma_phase);
         else if (dir == 2)
-          ok = pass_item<2, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin,
+          ok = pass_item<2, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, deferred, first_pass, last_pass, sm, dtmin,
                                        mbar, tma_phase);
         else
-          ok = pass_item<3, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, first_pass, last_pass, sm, dtmin,
+          ok = pass_item<3, RECON, RS>(a, B, w.x, l0, nc, Tc, constg, deferred, first_pass, last_pass, sm, dtmin,
                                        mbar, tma_phase);
         if (!ok) return;  // a TMA wait ran out (APH_ERR_TIMEOUT is recorded)
       }
     }
     if (!last_pass && !grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
   }
-  if (a.cf) {
+  if (a.cf) {  // the coarse-fine boundary cells, once every block's face fluxes are kept
     if (!grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
-    amr_correct(a, sched, ctr + 6);
-    if (!grid_barrier(a.ctl, a.timeout_ns, gridDim.x)) return;
-    amr_update(a, sched, ctr + 7, dtmin);
+    amr_fix(a, sched, ctr + 6, dtmin);
   }
   if (a.last) {
     dtmin = block_min(dtmin);

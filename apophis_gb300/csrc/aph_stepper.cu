@@ -153,7 +153,7 @@ struct aph_stepper_s {
   double *d_u1 = nullptr, *d_prim = nullptr, *d_gamma = nullptr, *d_du = nullptr;
   double *d_eraw = nullptr, *d_efl = nullptr;  // energy before / after the step-end floors
   double *d_backup = nullptr;  // autotuner state backup
-  int *d_flags = nullptr;
+  unsigned long long *d_flags = nullptr;  // block flags, then the launch counter (StageArgs)
   StepCtl *d_ctl = nullptr;
   int2 *d_cell_items = nullptr;
   int ncell_items = 0;
@@ -318,32 +318,12 @@ aph_status configure(aph_stepper s) {
   const int nb = p.nblocks;
   // lines per item and shared memory per direction
   const size_t smem = stage_lines(s, s->cfg.lines, s->cfg.tma != 0, s->T);
-  for (int d = 0; d < p.ndim; ++d) {
-    const int T = s->T[d];
-    std::vector<int2> items;
-    // schedule order: largest blocks first (longest-processing-time) so that the tail of a
-    // pass holds the small items
-    std::vector<int> order(nb);
-    for (int b = 0; b < nb; ++b) order[b] = b;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-      return s->hblocks[x].nint > s->hblocks[y].nint;
-    });
-    for (int b : order) {
-      const StepBlock &B = s->hblocks[b];
-      const int ntr = d == 0 ? B.nx[1] * B.nx[2] : d == 1 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1];
-      for (int l = 0; l < ntr; l += T) items.push_back(make_int2(b, l));
-    }
-    s->nline_items[d] = (int)items.size();
-    if (aph_status st = upload_items(s, &s->d_line_items[d], items)) return st;
-  }
+  auto smem_of = [&](int n, int T) {
+    return s->params.exact ? aph_exact::stage_smem_bytes(s->params.recon, n, T, p.nvar)
+                           : aph_fast::stage_smem_bytes(s->params.recon, n, T, p.nvar);
+  };
   if (smem > 220 * 1024)
     return fail(APH_ERR_UNSUPPORTED, "stage needs %zu bytes of shared memory; use fewer lines", smem);
-  if (s->cfg.tma) {
-    if (const char *why = tma_unsupported(s, s->T))
-      return fail(APH_ERR_UNSUPPORTED, "TMA windows need other lines per item or blocks: %s", why);
-    if (aph_status st = encode_tmaps(s)) return st;
-  }
-  s->smem = smem;
   const int threads = s->cfg.threads;
   int per_sm = stage_residency(s, threads, s->cfg.reg_cap, smem);
   if (per_sm < 1) return fail(APH_ERR_UNSUPPORTED, "stage kernel does not fit on an SM");
@@ -351,6 +331,54 @@ aph_status configure(aph_stepper s) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  std::vector<int> order(nb);  // largest blocks first
+  for (int b = 0; b < nb; ++b) order[b] = b;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return s->hblocks[x].nint > s->hblocks[y].nint;
+  });
+  for (int d = 0; d < p.ndim; ++d) {
+    const int T = s->T[d];
+    struct Item { int2 w; long long cost; };
+    std::vector<Item> list;
+    for (int b : order) {
+      const StepBlock &B = s->hblocks[b];
+      const int n = B.nx[d];
+      const int ntr = d == 0 ? B.nx[1] * B.nx[2] : d == 1 ? B.nx[0] * B.nx[2] : B.nx[0] * B.nx[1];
+      if (ntr >= (1 << (31 - kItemLineBits)) || T >= (1 << kItemLineBits))
+        return fail(APH_ERR_UNSUPPORTED, "block %d: %d lines along x%d, %d per item: too many", b, ntr,
+                    d + 1, T);
+      auto add = [&](int first, int lines) {
+        list.push_back(Item{make_int2(b, (first << kItemLineBits) | lines), (long long)lines * n});
+      };
+      if (s->cfg.tma) {  // the TMA box's T lines, the block's last item shorter
+        for (int l = 0; l < ntr; l += T) add(l, std::min(T, ntr - l));
+        continue;
+      }
+      // plain loads: a narrower block takes as many lines per item as the shared memory
+      // sized for the widest holds, and its lines are spread evenly over the fewest items
+      int Tb = std::min(T, ntr);
+      while (Tb < ntr && Tb + 1 < (1 << kItemLineBits) && smem_of(n, Tb + 1) <= smem) ++Tb;
+      const int k = (ntr + Tb - 1) / Tb, base = ntr / k, rem = ntr % k;
+      for (int i = 0, l = 0; i < k; ++i) {
+        const int lines = base + (i < rem ? 1 : 0);
+        add(l, lines);
+        l += lines;
+      }
+    }
+    // schedule order: the costliest items first (longest-processing-time), so that the tail
+    // of a pass holds the cheap ones
+    std::stable_sort(list.begin(), list.end(), [](const Item &x, const Item &y) { return x.cost > y.cost; });
+    std::vector<int2> items(list.size());
+    for (size_t i = 0; i < list.size(); ++i) items[i] = list[i].w;
+    s->nline_items[d] = (int)items.size();
+    if (aph_status st = upload_items(s, &s->d_line_items[d], items)) return st;
+  }
+  if (s->cfg.tma) {
+    if (const char *why = tma_unsupported(s, s->T))
+      return fail(APH_ERR_UNSUPPORTED, "TMA windows need other lines per item or blocks: %s", why);
+    if (aph_status st = encode_tmaps(s)) return st;
+  }
+  s->smem = smem;
   // entire-domain cell chunks
   std::vector<int2> cells;
   for (int b = 0; b < nb; ++b)
@@ -541,9 +569,11 @@ __global__ void k_set_dt(StepCtl *c, MemberCtl *m, int n, const double *dt) {
   }
 }
 
-__global__ void k_or_flags(const int *flags, int n, int *out) {
+// Whether the stage launch just run applied a floor in any block.
+__global__ void k_or_flags(const unsigned long long *flags, int n, int *out) {
+  const unsigned long long launch = flags[2 * n];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    if (flags[i]) atomicOr(out, 1);
+    if (launch != 0 && flags[2 * i] == launch) atomicOr(out, 1);
 }
 
 }  // namespace
@@ -588,7 +618,8 @@ cudaError_t stepper_step_dt(aph_stepper s, const double *dt_dev, double *keep, i
   const size_t field = stepper_field_doubles(s);
   for (size_t i = 0; i < stages.size() && e == cudaSuccess; ++i) {
     const int recon = (s->integrator == APH_INTEGRATOR_VL2 && i == 0) ? APH_RECON_DC : s->params.recon;
-    const StageArgs a = stage_args(s, (int)i, stages[i], false, false);
+    StageArgs a = stage_args(s, (int)i, stages[i], false, false);
+    a.full_domain = keep ? 1 : 0;  // the kept primitives are read over the entire domain
     e = launch_one(s, a, recon, st);
     if (e == cudaSuccess && keep)
       e = cudaMemcpyAsync(keep + i * field, s->d_prim, field * sizeof(double), cudaMemcpyDeviceToDevice, st);
@@ -771,7 +802,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
   ck(cudaMalloc(&s->d_du, sizeof(double) * nvar * inter));
   ck(cudaMalloc(&s->d_eraw, sizeof(double) * cells));
   ck(cudaMalloc(&s->d_efl, sizeof(double) * cells));
-  ck(cudaMalloc(&s->d_flags, sizeof(int) * p.nblocks));
+  ck(cudaMalloc(&s->d_flags, sizeof(unsigned long long) * (2 * (size_t)p.nblocks + 1)));
   ck(cudaMalloc(&s->d_ctl, sizeof(StepCtl)));
   ck(cudaMalloc(&s->d_blocks, sizeof(StepBlock) * p.nblocks));
   if (ens) {
@@ -817,7 +848,7 @@ aph_status aph_stepper_create(const aph_stepper_desc *desc, aph_stepper *out) {
     oi += B.nint;
   }
   ck(cudaMemcpy(s->d_blocks, s->hblocks.data(), sizeof(StepBlock) * p.nblocks, cudaMemcpyHostToDevice));
-  ck(cudaMemset(s->d_flags, 0, sizeof(int) * p.nblocks));
+  ck(cudaMemset(s->d_flags, 0, sizeof(unsigned long long) * (2 * (size_t)p.nblocks + 1)));
   ck(cudaMemset(s->d_efl, 0xff, sizeof(double) * cells));
   k_ctl_init<<<1, 1>>>(s->d_ctl, desc->tlim > 0 ? desc->tlim : DBL_MAX, desc->fixed_dt);
   ck(cudaGetLastError());

@@ -318,7 +318,9 @@ aph_status aph_diag_barrier_timeout(double timeout_s, void *stream);
 aph_status aph_diag_exact_ops(int op, const double *x, double *out, long long n, void *stream);
 /* The same for the integer-pipe IEEE additions and small multiplications: op 0: x + y,
  * 1: x - y, 2: 3 * x, 3: 6 * x, 4: 1.25 * x (y unused by ops 2-4), for operands zero or normal
- * with 2^-900 < |x| < 2^900. */
+ * with 2^-900 < |x| < 2^900; and for the FP64 pipe's operations they are weighed against:
+ * 5: x / y, 6: the reciprocal 1 / y, 7: sqrt(x), 8: x / y from the reciprocal of y (Markstein's
+ * correction, for x and y tame). */
 aph_status aph_diag_exact_ops2(int op, const double *x, const double *y, double *out, long long n,
                                void *stream);
 

@@ -6,7 +6,8 @@ range and on values made to put x / 6 close to a representable number or to a mi
 between two (where a faithful but incorrectly rounded quotient would show); half_x and
 twice_x on the range reachable from tame windows, zeros of both signs included; tame on
 values at and around its thresholds; the integer-pipe IEEE additions (add_x, sub_x) and
-multiplications by 3, 6 and 5/4 (mulk_x) on their whole stated range.
+multiplications by 3, 6 and 5/4 (mulk_x) on their whole stated range; the quotient from a
+correctly rounded reciprocal (div_rcp) on tame operands.
 """
 import ctypes
 
@@ -123,3 +124,28 @@ def test_integer_pipe_small_multiplies_match_ieee(cuda):
     x = np.concatenate([_random_in_range(rng, 2_000_000, -800, 800), np.array([0.0, -0.0, 1.0])])
     for op, k in ((2, 3.0), (3, 6.0), (4, 1.25)):
         _bits_equal(_run2(op, x, x), k * x, "x%g" % k)
+
+
+def test_quotient_from_reciprocal_matches_ieee_division(cuda):
+    """x / y from y's correctly rounded reciprocal (Markstein's correction) against IEEE
+    division: random tame pairs, quotients made to fall within a few ulps of a representable
+    number or of a midpoint between two (where a faithful but incorrectly rounded quotient
+    would show), exact integer quotients and signed zeros."""
+    rng = np.random.Generator(np.random.PCG64(9))
+    n = 3_000_000
+    a = _random_in_range(rng, n, -200, 200)
+    b = _random_in_range(rng, n, -200, 200)
+    q = _random_in_range(rng, n, -150, 150)
+    mid = q + np.spacing(q) * 0.5  # rounds to a neighbour of the midpoint
+    near = []
+    for c in (q, mid):
+        x = (c * b).view(np.int64) + rng.integers(-3, 4, n)
+        near.append(x.view(np.float64))
+    ints = np.arange(-300, 301, dtype=np.float64)
+    ints = ints[ints != 0]
+    xs = np.concatenate([a] + near + [np.repeat(ints, ints.size), np.array([0.0, -0.0, 0.0, -0.0])])
+    ys = np.concatenate([b, b, b, np.tile(ints, ints.size), np.array([3.0, 3.0, -3.0, -3.0])])
+    keep = (np.abs(xs) >= 2.0 ** -200) & (np.abs(xs) < 2.0 ** 201) | (xs == 0)
+    xs, ys = xs[keep], ys[keep]
+    _bits_equal(_run2(8, xs, ys), xs / ys, "x / y by the reciprocal")
+    _bits_equal(_run2(5, xs, ys), xs / ys, "x / y")
