@@ -334,9 +334,17 @@ __global__ void k_c2p_vjp(AdjGeom g, const double *w, const double *lam_w, doubl
   if (c >= g.ncell) return;
   const long long o = blk_off(g, b), nc = g.ncell;
   double ww[5], gw[5], gu[5];
+  bool flows = false;
   for (int v = 0; v < 5; ++v) {
     ww[v] = w[o + v * nc + c];
     gw[v] = lam_w[o + v * nc + c];
+    flows |= (__double_as_longlong(gw[v]) << 1) != 0;
+  }
+  // the map is linear in gw: a cell no pass reads (whose primitives the forward may not have
+  // formed, e.g. a ghost corner of a finished member's block) gets exactly zero
+  if (!flows) {
+    for (int v = 0; v < 5; ++v) lam_u[o + v * nc + c] = 0.0;
+    return;
   }
   cons_to_prim_vjp(ww, gw, g.mem[g.blk[b].member].gc.gm1, gu);
   for (int v = 0; v < 5; ++v) lam_u[o + v * nc + c] = gu[v];

@@ -159,6 +159,39 @@ def test_ensemble_adjoint_matches_members_alone(cuda):
     ea.close()
 
 
+def test_ensemble_adjoint_member_finished_early(cuda):
+    """A member past its end time (dt 0, its blocks skipped) while segments are recomputed:
+    the batched reverse sweep stays finite and equals each member's own sweep over the steps
+    it took (the skipped blocks' primitives include cells no pass ever formed)."""
+    import torch
+    from apophis_gb300.adjoint import Adjoint, EnsembleAdjoint
+    ens, conses = _adjoint_ensemble(seed=5)
+    nsteps, done0 = 6, 2
+    dts = [[0.15 * c.dx[0] if (m > 0 or k < done0) else 0.0 for m, c in enumerate(ens.members)]
+           for k in range(nsteps)]
+    flat = torch.from_numpy(ens.pack(conses)).cuda()
+    gen = torch.Generator(device="cuda").manual_seed(12)
+    lam = torch.randn(flat.shape, dtype=torch.float64, device="cuda", generator=gen)
+    ea = EnsembleAdjoint(ens)
+    ea.forward_members(flat, dts, checkpoint_every=2)
+    lam0_h = ea.backward(lam).cpu().numpy()
+    lam_h = lam.cpu().numpy()
+    assert np.isfinite(lam0_h).all()
+    for m, cfg in enumerate(ens.members):
+        a = Adjoint(cfg)
+        u0m = torch.from_numpy(np.ascontiguousarray(conses[m])).cuda()
+        steps = [r[m] for r in dts if r[m] > 0.0]
+        a.forward(u0m, steps, 2)
+        lm = torch.from_numpy(np.ascontiguousarray(ens.unpack(lam_h, m))).cuda()
+        want = a.backward(lm).cpu().numpy()
+        got = ens.unpack(lam0_h, m)
+        sk, sj, si = cfg.interior
+        err = np.abs(got[:, :, sk, sj, si] - want[:, :, sk, sj, si]).max() / np.abs(want).max()
+        assert err <= 1e-13, (m, err)
+        a.close()
+    ea.close()
+
+
 def test_ensemble_pressure_gradient_fd(cuda):
     """Gradient of L = sum_m ||rho_m(T)||^2 / 2 with respect to every member's initial pressure
     (one batched reverse sweep), against central differences on seeded directions.
