@@ -66,11 +66,11 @@ BYTES_PER_ZONE_UPDATE = 200.0   # RK2 with 5 FP64 conserved variables
 # FP64 work of the stage kernel per RK2 zone-update on this workload: the DADD + DMUL + DFMA
 # thread instructions the kernel executes (ncu sass counters of one stage launch of each kind
 # on a 128^3 pack of 64^3 blocks, per zone), by arithmetic mode
-FP64_LANE_OPS_PER_ZONE_UPDATE = {"fast": 1981.0, "exact": 2487.0}
+FP64_LANE_OPS_PER_ZONE_UPDATE = {"fast": 1981.0, "exact": 2365.0}
 FP64_LANES_PER_CLK_PER_SM = 2.0    # DFMA lanes per clock per SM on GB300 (measured)
 # DRAM bytes (read + write) per zone per stage launch, same captures (the 256^3 launches
 # process 8x the blocks of the 128^3 capture, so traffic is scaled by zones)
-TRAFFIC_BYTES_PER_ZONE_LAUNCH = {"fast": 628.3, "exact": 689.1}
+TRAFFIC_BYTES_PER_ZONE_LAUNCH = {"fast": 628.3, "exact": 663.4}
 TRAFFIC_LAUNCH = {"fast": "8 lines, dynamic schedule (not the tuned launch)",
                   "exact": "256 threads, 3 lines, dynamic schedule, 80-register build: the tuned launch"}
 PARITY = {
@@ -210,7 +210,13 @@ def amr_leg(args, warmup):
         return a.elapsed_time(b) / n
 
     st = amr.AmrStepper(cfg, cons, exact=args.exact)
-    tune = None if args.no_tune else st.autotune(trial_steps=2)
+    if args.launch:  # a given launch configuration, as for the headline
+        c = st.config
+        c.update(json.loads(args.launch))
+        st.set_config(c)
+        tune = {"config": st.config}
+    else:
+        tune = None if args.no_tune else st.autotune(trial_steps=2)
     st.step(warmup)
     st.status()
     stage_ms = st.profile(nsteps=2)
@@ -558,7 +564,7 @@ def main():
     ap.add_argument("--no-amr", action="store_true", help="skip the refined-pack leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint ratio leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the blast-ensemble leg")
-    ap.add_argument("--only", choices=["amr", "ensemble", "adjoint", "table"],
+    ap.add_argument("--only", choices=["amr", "ensemble", "adjoint", "ensemble_adjoint", "table"],
                     help="run one extra leg alone and print its object (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -570,7 +576,8 @@ def main():
         _build.build()
         args.exact = exact
         out = {"amr": lambda: amr_leg(args, args.warmup), "ensemble": lambda: ensemble_leg(args),
-               "adjoint": adjoint_leg, "table": lambda: table_leg(args)}[args.only]()
+               "adjoint": adjoint_leg, "ensemble_adjoint": ensemble_adjoint_leg,
+               "table": lambda: table_leg(args)}[args.only]()
         print(json.dumps({"only": args.only, args.only: out}), flush=True)
         return
 
