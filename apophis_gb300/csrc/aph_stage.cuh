@@ -259,6 +259,78 @@ __device__ __forceinline__ bool pass_reads(const PackDev &p, const StepBlock &B,
   return out == 1 && depth <= G;
 }
 
+// Whether the face ghost cell (i, j, k) of B holds a copy of an interior cell: a same-level
+// neighbour's (on a uniform block grid always, periodic wraps included), or B's own at an
+// outflow or reflecting boundary -- rather than values formed by restriction or prolongation
+// at a coarse-fine face.  ConsToPrim of a copy equals the source cell's primitives (with the
+// normal velocity negated at a reflecting boundary: IEEE products are sign-symmetric), so the
+// passes read those at the source (ghost_copy_src) and phase 1 leaves such ghosts alone.
+__device__ __forceinline__ bool ghost_is_copy(const PackDev &p, const StepBlock &B, int i, int j, int k) {
+  if (!p.amr) return true;
+  const int e[3] = {i, j, k};
+  int face = 0;
+  for (int d = 0; d < p.ndim; ++d) {
+    const int x = e[d] - p.ng;
+    if (x < 0) face = 2 * d;
+    else if (x >= B.nx[d]) face = 2 * d + 1;
+  }
+  return B.amr.kind[face] == FACE_SAME || B.amr.kind[face] == FACE_BOUNDARY;
+}
+
+// The source of the copied ghost cell at position c (c < 0 or c >= n) along DIR of line l of
+// B (base, stride: the line's first interior cell and its step): the block S, its cell sc and
+// the velocity component to negate (flipv, -1: none).  Leaves them untouched and returns
+// false for a ghost formed at a coarse-fine face.
+template <int DIR>
+__device__ __forceinline__ bool ghost_copy_src(const StageArgs &a, const StepBlock &B, int l, int c,
+                                               long long base, long long stride, const StepBlock *&S,
+                                               long long &sc, int &flipv) {
+  const PackDev &p = a.p;
+  constexpr int d = DIR - 1;
+  const int n = B.nx[d];
+  if (!p.amr) {  // the uniform block grid's map (ghost_cell)
+    bool flip = false;
+    const int g = map_index(B.loc[d] * n + c, p.mesh_nx[d], p.bc[d][0], p.bc[d][1], flip);
+    const int sl = g / n;
+    int loc[3] = {B.loc[0], B.loc[1], B.loc[2]};
+    loc[d] = sl;
+    S = &a.blocks[(loc[2] * p.nb[1] + loc[1]) * p.nb[0] + loc[0]];
+    sc = base + (long long)(g - sl * n) * stride;
+    flipv = flip ? IV1 + d : -1;
+    return true;
+  }
+  if (d > 1) return false;  // face tables are 2D
+  const int side = c < 0 ? 0 : 1, depth = c < 0 ? -c - 1 : c - n;
+  const int face = 2 * d + side, td = 1 - d;
+  const int kind = B.amr.kind[face];
+  if (kind == FACE_SAME) {  // as amr_ghost5; the line index is the transverse coordinate
+    const StepBlock &N = a.blocks[B.amr.nbr[face][0]];
+    S = &N;
+    sc = amr_cell(N, p.ng, d, side == 0 ? N.nx[d] - 1 - depth : depth, B.amr.origin[td] + l - N.amr.origin[td]);
+    flipv = -1;
+    return true;
+  }
+  if (kind == FACE_BOUNDARY) {
+    S = &B;
+    if (p.bc[d][side] == 1) {  // outflow
+      sc = amr_cell(B, p.ng, d, side == 0 ? 0 : n - 1, l);
+      flipv = -1;
+    } else {                   // reflecting
+      sc = amr_cell(B, p.ng, d, side == 0 ? depth : n - 1 - depth, l);
+      flipv = IV1 + d;
+    }
+    return true;
+  }
+  return false;
+}
+
+// Copied ghosts come from their sources unless the launch stages windows by TMA (which copies
+// each block's own ghost cells), the caller filled the ghosts (a halo exchange) or the
+// primitives of the entire domain are kept (the adjoint).
+__device__ __forceinline__ bool ghosts_from_sources(const StageArgs &a) {
+  return !a.full_domain && !a.ghosts_given && !a.tmaps;
+}
+
 __device__ __forceinline__ unsigned long long block_min(unsigned long long v) {
   __shared__ unsigned long long red[32];
 #pragma unroll
@@ -517,40 +589,50 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
     }
   } else {
     const int per = nl * NW;
-    for (int it = tid; it < V * per; it += nth) {
-      const int v = it / per;
-      const int r = it - v * per;
+    const bool src_ghosts = ghosts_from_sources(a);
+    // per window cell: its line geometry and source once, then its V values
+    for (int it = tid; it < per; it += nth) {
       int t, w;
-      if (DIR == 1) { t = r / NW; w = r - t * NW; } else { w = r / nl; t = r - w * nl; }
+      if (DIR == 1) { t = it / NW; w = it - t * NW; } else { w = it / nl; t = it - w * nl; }
       long long base, stride, ib, is;
       line_of<DIR>(B, a.p.ndim, a.p.ng, l0 + t, base, stride, ib, is);
-      const long long cell = base + (long long)(w - G) * stride;
-      double x;
-      if (v < nv) {
-        x = B.prim[v * nc + cell];
-      } else {
+      const int c = w - G;
+      long long cell = base + (long long)c * stride;
+      const StepBlock *S = &B;  // the block holding the cell's primitives
+      int flipv = -1;
+      if (src_ghosts && (c < 0 || c >= n)) ghost_copy_src<DIR>(a, B, l0 + t, c, base, stride, S, cell, flipv);
+      const long long snc = S->ncell;
+      for (int v = 0; v < nv; ++v) {
+        const double x = flip_if(S->prim[v * snc + cell], v == flipv);
+        W[((size_t)v * T + t) * NW + w] = x;
 #if APH_EXACT
-        x = B.gamma[(v - nv) * nc + cell];
+        tame_ok = tame_ok && tame(x);
+#endif
+      }
+      if (V > nv) {
+        double g_c, g_e;
+#if APH_EXACT
+        g_c = S->gamma[cell];
+        g_e = S->gamma[snc + cell];
+        tame_ok = tame_ok && tame(g_c) && tame(g_e);
 #else
         // the fast ConsToPrim leaves the constants where no floor fired; the reference's
         // values (which the limiters see) are recomputed from the cell's state there (a
         // floored cell's state may still wait in du for the first pass to store it)
-        if (__double_as_longlong(B.prim[IPR * nc + cell]) == __double_as_longlong(a.p.pfloor) ||
-            __double_as_longlong(B.prim[IDN * nc + cell]) == __double_as_longlong(a.p.dfloor)) {
-          x = B.gamma[(v - nv) * nc + cell];  // floored: the reference's values already
+        if (__double_as_longlong(S->prim[IPR * snc + cell]) == __double_as_longlong(a.p.pfloor) ||
+            __double_as_longlong(S->prim[IDN * snc + cell]) == __double_as_longlong(a.p.dfloor)) {
+          g_c = S->gamma[cell];  // floored: the reference's values already
+          g_e = S->gamma[snc + cell];
         } else {
-          double uc[NHYDRO], g_c, g_e;
+          double uc[NHYDRO];
 #pragma unroll
-          for (int k = 0; k < NHYDRO; ++k) uc[k] = B.u0[k * nc + cell];
+          for (int k = 0; k < NHYDRO; ++k) uc[k] = S->u0[k * snc + cell];
           gamma_ref(uc, gc.gm1, g_c, g_e);
-          x = v == nv ? g_c : g_e;
         }
 #endif
+        W[((size_t)nv * T + t) * NW + w] = g_c;
+        W[((size_t)(nv + 1) * T + t) * NW + w] = g_e;
       }
-      W[((size_t)v * T + t) * NW + w] = x;
-#if APH_EXACT
-      tame_ok = tame_ok && tame(x);
-#endif
     }
   }
 #if APH_EXACT
@@ -906,6 +988,7 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
     // the passes read ghost cells only along their lines, at most G cells beyond the interior:
     // the others (edges, corners, the layers beyond G) are neither filled nor converted
     if (!inner && !a.full_domain && !pass_reads(p, B, i, j, k, Halo<RECON>::G)) continue;
+    if (!inner && ghosts_from_sources(a) && ghost_is_copy(p, B, i, j, k)) continue;
     if (!inner && !a.ghosts_given) {  // the ghost values of u0 (read back below by this thread)
       if (p.amr) {
         const bool start = a.copy_u1;

@@ -247,7 +247,8 @@ def test_ensemble_pressure_gradient_fd(cuda):
 
 
 def test_ensemble_tma_windows_match_plain_loads(cuda):
-    """Equal blocks across members: the TMA-staged windows give the same bits."""
+    """Equal blocks across members: the TMA-staged windows give the same bits (interiors:
+    ghost cells hold stage inputs, which plain-load launches read at their sources)."""
     ens, conses, flat = small_ensemble()
     outs = []
     for tma in (0, 1):
@@ -257,4 +258,9 @@ def test_ensemble_tma_windows_match_plain_loads(cuda):
         st.step(4)
         outs.append((st.state(), st.member_status()))
         st.close()
-    assert np.array_equal(outs[0][0], outs[1][0]) and outs[0][1] == outs[1][1]
+    assert outs[0][1] == outs[1][1]
+    for m, cfg in enumerate(ens.members):
+        sk, sj, si = cfg.interior
+        a = ens.unpack(outs[0][0], m)[:, :, sk, sj, si]
+        b = ens.unpack(outs[1][0], m)[:, :, sk, sj, si]
+        assert np.array_equal(a, b), m
