@@ -479,39 +479,54 @@ __device__ __forceinline__ void ppm_window(const double *W, double *D2, double *
                                            int G) {
   const int NW = n + 2 * G;
   const int tid = threadIdx.x, nth = blockDim.x;
-  auto w_at = [&](int v, int t, int c) -> double { return W[((size_t)v * T + t) * NW + c + G]; };
+  // row v * T + t of the slabs and position i in it, for element it of rows of width w (one
+  // division where the item fills its T lines, as plain-load items do)
+  const bool full = nl == T;
+  auto decode = [&](int it, int w, int &row, int &i) {
+    if (full) {
+      row = it / w;
+      i = it - row * w;
+    } else {
+      const int v = it / (nl * w);
+      const int r = it - v * nl * w;
+      const int t = r / w;
+      i = r - t * w;
+      row = v * T + t;
+    }
+  };
+  auto w_at = [&](int row, int c) -> double { return W[(size_t)row * NW + c + G]; };
   const int w4 = n + 4, w3 = n + 3;
   for (int it = tid; it < V * nl * w4; it += nth) {  // cells -2..n+1
-    const int v = it / (nl * w4);
-    const int r = it - v * nl * w4;
-    const int t = r / w4, c = r - t * w4 - 2;
-    const double qm = w_at(v, t, c - 1), q0 = w_at(v, t, c), qp = w_at(v, t, c + 1);
-    D2[((size_t)v * T + t) * w4 + c + 2] = ppm_d2<TAME>(qm, q0, qp);
-    DD[((size_t)v * T + t) * w4 + c + 2] = ppm_dd<TAME>(qm, q0, qp);
+    int row, i;
+    decode(it, w4, row, i);
+    const int c = i - 2;
+    const double qm = w_at(row, c - 1), q0 = w_at(row, c), qp = w_at(row, c + 1);
+    D2[(size_t)row * w4 + c + 2] = ppm_d2<TAME>(qm, q0, qp);
+    DD[(size_t)row * w4 + c + 2] = ppm_dd<TAME>(qm, q0, qp);
   }
   __syncthreads();
   for (int it = tid; it < V * nl * w3; it += nth) {  // faces -1..n+1
-    const int v = it / (nl * w3);
-    const int r = it - v * nl * w3;
-    const int t = r / w3, f = r - t * w3 - 1;
-    const size_t o = ((size_t)v * T + t) * w4;
-    DPH[((size_t)v * T + t) * w3 + f + 1] =
-        ppm_face<TAME>(w_at(v, t, f - 1), w_at(v, t, f), DD[o + f + 1], DD[o + f + 2],
+    int row, i;
+    decode(it, w3, row, i);
+    const int f = i - 1;
+    const size_t o = (size_t)row * w4;
+    DPH[(size_t)row * w3 + f + 1] =
+        ppm_face<TAME>(w_at(row, f - 1), w_at(row, f), DD[o + f + 1], DD[o + f + 2],
                        D2[o + f + 1], D2[o + f + 2]);
   }
   __syncthreads();
   const int w2 = n + 2;
   for (int it = tid; it < V * nl * w2; it += nth) {  // cells -1..n
-    const int v = it / (nl * w2);
-    const int r = it - v * nl * w2;
-    const int t = r / w2, c = r - t * w2 - 1;
-    const size_t o4 = ((size_t)v * T + t) * w4, o3 = ((size_t)v * T + t) * w3;
+    int row, i;
+    decode(it, w2, row, i);
+    const int c = i - 1;
+    const size_t o4 = (size_t)row * w4, o3 = (size_t)row * w3;
     double ql, qr;
-    ppm_cell<TAME>(w_at(v, t, c - 2), w_at(v, t, c - 1), w_at(v, t, c), w_at(v, t, c + 1),
-                   w_at(v, t, c + 2), D2[o4 + c + 1], D2[o4 + c + 2], D2[o4 + c + 3],
+    ppm_cell<TAME>(w_at(row, c - 2), w_at(row, c - 1), w_at(row, c), w_at(row, c + 1),
+                   w_at(row, c + 2), D2[o4 + c + 1], D2[o4 + c + 2], D2[o4 + c + 3],
                    DPH[o3 + c + 1], DPH[o3 + c + 2], ql, qr);
-    SL[((size_t)v * T + t) * w2 + c + 1] = ql;
-    SR[((size_t)v * T + t) * w2 + c + 1] = qr;
+    SL[(size_t)row * w2 + c + 1] = ql;
+    SR[(size_t)row * w2 + c + 1] = qr;
   }
 }
 
@@ -738,16 +753,16 @@ __device__ bool pass_item(const StageArgs &a, const StepBlock &B, int b, int l0,
     const size_t fs = (size_t)T * w1;
     const double area = DIR == 1 ? B.dx[1] * B.dx[2] : DIR == 2 ? B.dx[0] * B.dx[2] : B.dx[0] * B.dx[1];
     if (!last_pass) {
-      for (int it = tid; it < nv * nl * n; it += nth) {
-        const int v = it / (nl * n);
-        const int r = it - v * nl * n;
-        const int t = r / n, c = r - t * n;
+      for (int it = tid; it < nl * n; it += nth) {  // per cell: its geometry once, then its nv values
+        const int t = it / n, c = it - t * n;
         long long base, stride, ib, is;
         line_of<DIR>(B, a.p.ndim, a.p.ng, l0 + t, base, stride, ib, is);
-        const size_t of = v * fs + (size_t)t * w1 + c;
-        const double d = (area * F[of + 1] - area * F[of]);
-        double *du = B.du + v * B.nint + ib + c * is;
-        *du = first_pass ? d : *du + d;
+        double *du = B.du + ib + c * is;
+        for (int v = 0; v < nv; ++v) {
+          const size_t of = v * fs + (size_t)t * w1 + c;
+          const double d = (area * F[of + 1] - area * F[of]);
+          du[v * B.nint] = first_pass ? d : du[v * B.nint] + d;
+        }
       }
     } else {
       const double vol = B.dx[0] * B.dx[1] * B.dx[2];
