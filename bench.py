@@ -66,11 +66,11 @@ BYTES_PER_ZONE_UPDATE = 200.0   # RK2 with 5 FP64 conserved variables
 # FP64 work of the stage kernel per RK2 zone-update on this workload: the DADD + DMUL + DFMA
 # thread instructions the kernel executes (ncu sass counters of one stage launch of each kind
 # on a 128^3 pack of 64^3 blocks, per zone), by arithmetic mode
-FP64_LANE_OPS_PER_ZONE_UPDATE = {"fast": 1981.0, "exact": 2365.0}
+FP64_LANE_OPS_PER_ZONE_UPDATE = {"fast": 1981.0, "exact": 2364.0}
 FP64_LANES_PER_CLK_PER_SM = 2.0    # DFMA lanes per clock per SM on GB300 (measured)
 # DRAM bytes (read + write) per zone per stage launch, same captures (the 256^3 launches
 # process 8x the blocks of the 128^3 capture, so traffic is scaled by zones)
-TRAFFIC_BYTES_PER_ZONE_LAUNCH = {"fast": 628.3, "exact": 663.4}
+TRAFFIC_BYTES_PER_ZONE_LAUNCH = {"fast": 628.3, "exact": 612.7}
 TRAFFIC_LAUNCH = {"fast": "8 lines, dynamic schedule (not the tuned launch)",
                   "exact": "256 threads, 3 lines, dynamic schedule, 80-register build: the tuned launch"}
 PARITY = {
