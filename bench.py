@@ -730,6 +730,8 @@ def main():
         ach = ops * zones / (stage_sum * 1e-3) / 1e9
         line["fp64_pipe"].update({"achieved": ach, "peak": fp64_peak, "unit": "G lane-ops/s",
                                   "frac": ach / fp64_peak, "ops_per_zone_update": ops})
+        # the bound that binds, beside the HBM figures of the roofline object
+        line["roofline"]["fp64_pipe_frac"] = ach / fp64_peak
     if other is not None:
         line["other_mode"] = other
     if plain is not None:
