@@ -201,9 +201,11 @@ aph_status aph_hydro_fill_ghosts(aph_pack pack, void *stream);
  * stage is one persistent launch over every meshblock (ghost fill, ConsToPrim, the
  * x/y/z flux passes, the update, gravity and, at the last stage, the dt reduction);
  * dt and time stay on the device; a step is captured once as a CUDA graph and replayed.
- * The state is the caller's cons (u0); the stepper owns u1 and its scratch.  The floors
- * of the last FillDerived of a step are applied at the start of the next stage, so cons
- * between steps holds the update's raw values. */
+ * The state is the caller's cons (u0): its interior cells; the stepper owns u1 and its
+ * scratch.  Ghost cells of cons are scratch too: a stage forms the ghost values it reads (a
+ * ghost that copies an interior cell is read at that cell and not written), so between steps
+ * they hold no defined values.  The floors of the last FillDerived of a step are applied at
+ * the start of the next stage, so cons between steps holds the update's raw values. */
 typedef struct aph_stepper_s *aph_stepper;
 
 /* A batch of independent problems (an ensemble) stepped together in one pack: block b belongs
