@@ -3,6 +3,7 @@
 // replayed; plus the autotuner that picks CTA size, lines per work item, sweep order
 // and the CTA schedule.
 #include <algorithm>
+#include <utility>
 #include <cfloat>
 #include <chrono>
 #include <cmath>
@@ -1173,20 +1174,27 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
   cudaEventCreate(&e1);
   double best_t = 1e300;
   aph_stepper_config best_c = base;
+  std::vector<std::pair<double, aph_stepper_config>> timed;  // every candidate that ran
+  auto time_one = [&](const aph_stepper_config &c, int steps, double &per) {
+    if (aph_stepper_set_config(s, &c) != APH_OK) return false;
+    restore();
+    if (aph_stepper_step(s, 1, 0) != APH_OK) return false;  // warm-up (and graph build)
+    cudaEventRecord(e0, 0);
+    if (aph_stepper_step(s, steps, 0) != APH_OK) return false;
+    cudaEventRecord(e1, 0);
+    cudaEventSynchronize(e1);
+    StepCtl c2;
+    if (read_ctl(s, &c2) != APH_OK) return false;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    per = ms / steps;
+    return true;
+  };
   auto trial = [&](const std::vector<aph_stepper_config> &cands) {
     for (const aph_stepper_config &c : cands) {
-      if (aph_stepper_set_config(s, &c) != APH_OK) continue;
-      restore();
-      if (aph_stepper_step(s, 1, 0) != APH_OK) continue;  // warm-up (and graph build)
-      cudaEventRecord(e0, 0);
-      if (aph_stepper_step(s, trial_steps, 0) != APH_OK) continue;
-      cudaEventRecord(e1, 0);
-      cudaEventSynchronize(e1);
-      StepCtl c2;
-      if (read_ctl(s, &c2) != APH_OK) return;
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
-      const double per = ms / trial_steps;
+      double per;
+      if (!time_one(c, trial_steps, per)) continue;
+      timed.emplace_back(per, c);
       if (per < best_t) {
         best_t = per;
         best_c = c;
@@ -1244,10 +1252,12 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
     for (int d = 0; d < 3; ++d) c0.order[d] = d + 1;
     std::vector<aph_stepper_config> cands;
     for (int threads : {128, 256})
-      for (int rc : {0, 1}) {
-        const auto v = shapes(threads, rc, 0, c0);
-        cands.insert(cands.end(), v.begin(), v.end());
-      }
+      for (int rc : {0, 1})
+        for (aph_stepper_config c : shapes(threads, rc, 0, c0)) {
+          cands.push_back(c);  // strided, and the dynamic work counter (the pick can differ)
+          c.schedule = 2;
+          cands.push_back(c);
+        }
     if (cands.empty()) cands.push_back(c0);
     trial(cands);
   }
@@ -1282,6 +1292,26 @@ aph_status aph_stepper_autotune(aph_stepper s, int trial_steps, aph_stepper_conf
         cands.insert(cands.end(), v.begin(), v.end());
       }
     trial(cands);
+  }
+  // the three fastest candidates timed again over twice the steps (candidates within a few
+  // per cent of each other are otherwise picked by the noise of a short trial)
+  std::stable_sort(timed.begin(), timed.end(),
+                   [](const std::pair<double, aph_stepper_config> &x,
+                      const std::pair<double, aph_stepper_config> &y) { return x.first < y.first; });
+  if (timed.size() > 1) {
+    best_t = 1e300;
+    for (size_t i = 0; i < timed.size() && i < 3; ++i) {
+      double per;
+      if (!time_one(timed[i].second, 2 * trial_steps, per)) continue;
+      if (per < best_t) {
+        best_t = per;
+        best_c = timed[i].second;
+      }
+    }
+    if (best_t == 1e300) {  // none ran again: the first round's best
+      best_t = timed[0].first;
+      best_c = timed[0].second;
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
