@@ -117,7 +117,7 @@ struct StageArgs {
   const int *fix_items;         // refined meshes: blocks with a finer neighbour
   int nfix_items;
   int bflux_stride;             // doubles per face of bflux (max transverse cells * nvar)
-  int cf;                       // refined meshes with coarse-fine faces: correction phases
+  int cf;                       // refined meshes with coarse-fine faces: the coarse-fine phase
   MemberCtl *members;           // ensembles (NULL: one problem, clock in ctl)
   const void *tmaps;            // TMA: three tensor maps (x, y, z windows) over prim, or NULL
   int ext[3];                   // TMA: entire extents ni, nj, nk of every block
