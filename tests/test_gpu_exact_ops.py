@@ -16,6 +16,7 @@ import pytest
 import torch
 
 from apophis_gb300 import _capi, hydro
+from quotient_cases import midpoint_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -129,22 +130,24 @@ def test_integer_pipe_small_multiplies_match_ieee(cuda):
 def test_quotient_from_reciprocal_matches_ieee_division(cuda):
     """x / y from y's correctly rounded reciprocal (Markstein's correction) against IEEE
     division: random tame pairs, quotients made to fall within a few ulps of a representable
-    number or of a midpoint between two (where a faithful but incorrectly rounded quotient
-    would show), exact integer quotients and signed zeros."""
+    number, quotients within ~1e-14 ulp of a rounding midpoint (where a faithful but
+    incorrectly rounded quotient would show), exact integer quotients and signed zeros."""
     rng = np.random.Generator(np.random.PCG64(9))
     n = 3_000_000
     a = _random_in_range(rng, n, -200, 200)
     b = _random_in_range(rng, n, -200, 200)
     q = _random_in_range(rng, n, -150, 150)
-    mid = q + np.spacing(q) * 0.5  # rounds to a neighbour of the midpoint
+    # x near q y (and near (q + ulp(q) / 2) y), moved by a few ulps of x
     near = []
-    for c in (q, mid):
-        x = (c * b).view(np.int64) + rng.integers(-3, 4, n)
+    for x0 in (q * b, q * b + (np.spacing(q) * 0.5) * b):
+        x = x0.view(np.int64) + rng.integers(-3, 4, n)
         near.append(x.view(np.float64))
+    # quotients within ~1e-14 ulp of a rounding midpoint (the hardest cases of division)
+    ma, mb = midpoint_cases(rng, 50_000)
     ints = np.arange(-300, 301, dtype=np.float64)
     ints = ints[ints != 0]
-    xs = np.concatenate([a] + near + [np.repeat(ints, ints.size), np.array([0.0, -0.0, 0.0, -0.0])])
-    ys = np.concatenate([b, b, b, np.tile(ints, ints.size), np.array([3.0, 3.0, -3.0, -3.0])])
+    xs = np.concatenate([a] + near + [ma, np.repeat(ints, ints.size), np.array([0.0, -0.0, 0.0, -0.0])])
+    ys = np.concatenate([b, b, b, mb, np.tile(ints, ints.size), np.array([3.0, 3.0, -3.0, -3.0])])
     keep = (np.abs(xs) >= 2.0 ** -200) & (np.abs(xs) < 2.0 ** 201) | (xs == 0)
     xs, ys = xs[keep], ys[keep]
     _bits_equal(_run2(8, xs, ys), xs / ys, "x / y by the reciprocal")
