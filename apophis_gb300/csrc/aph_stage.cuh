@@ -1003,6 +1003,7 @@ __global__ void __launch_bounds__(kStageThreads, MINB) k_stage(StageArgs a) {
     // the passes read ghost cells only along their lines, at most G cells beyond the interior:
     // the others (edges, corners, the layers beyond G) are neither filled nor converted
     if (!inner && !a.full_domain && !pass_reads(p, B, i, j, k, Halo<RECON>::G)) continue;
+    // and a ghost that copies an interior cell is read at that cell (ghost_copy_src)
     if (!inner && ghosts_from_sources(a) && ghost_is_copy(p, B, i, j, k)) continue;
     if (!inner && !a.ghosts_given) {  // the ghost values of u0 (read back below by this thread)
       if (p.amr) {
